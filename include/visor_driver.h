@@ -1,0 +1,65 @@
+/*
+ * visor_driver.h - records a vsc_scene through the Vulkan API of an ICD.
+ *
+ * This is the application side of the boundary: it obtains every entry point
+ * from the ICD's vk_icdGetInstanceProcAddr (exactly as the Vulkan loader
+ * does, icd_interface.cpp:132-148), creates buffers, images, shader modules
+ * (SPIR-V from visor_spirv.h), pipelines, descriptor sets, render passes and
+ * framebuffers, records one command buffer per scene and submits it with
+ * vkQueueSubmit.  The same source drives this project's GPU ICD and the
+ * reference ICD built from its own sources (oracle/_ref).
+ */
+#ifndef VISOR_DRIVER_H
+#define VISOR_DRIVER_H
+
+#include <stdint.h>
+
+#include "visor_scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void (*vsd_void_fn)(void);
+typedef vsd_void_fn (*vsd_get_proc_fn)(void *instance, const char *name);
+
+typedef struct vsd_context vsd_context;
+typedef struct vsd_scene vsd_scene;
+
+enum {
+  VSD_RESTAGE_INPUTS = 1u << 0, /* re-copy vertex/index staging buffers into device memory every submit */
+  VSD_DEVICE_TARGETS = 1u << 1, /* render targets in device-local memory (no readback) */
+};
+
+/*
+ * Create instance, device and queue through `gpa`.  When `instance` is non-NULL
+ * it is used instead of calling vkCreateInstance (the reference's
+ * vkCreateInstance starts its raster thread pool; the serial oracle mode
+ * passes a pre-made handle).  Returns 0 on success, else the failing VkResult.
+ */
+int vsd_create(vsd_get_proc_fn gpa, void *instance, vsd_context **out);
+void vsd_destroy(vsd_context *ctx);
+
+/* Create every object the scene needs and record its command buffer. */
+int vsd_upload(vsd_context *ctx, const vsc_scene *scene, uint32_t flags, vsd_scene **out);
+
+/* vkQueueSubmit + vkWaitForFences.  Returns 0 or the failing VkResult. */
+int vsd_submit(vsd_scene *s);
+
+/* Submit only (the caller waits with vsd_wait). */
+int vsd_submit_async(vsd_scene *s);
+int vsd_wait(vsd_scene *s, uint64_t timeout_ns);
+
+/* Copy target t's colour (BGRA8) and depth (f32) out through vkMapMemory. */
+int vsd_read_target(vsd_scene *s, uint32_t target, uint8_t *color, float *depth);
+
+void vsd_release(vsd_scene *s);
+
+/* Bytes copied host->device per submit when VSD_RESTAGE_INPUTS is set. */
+uint64_t vsd_restage_bytes(const vsd_scene *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,198 @@
+/*
+ * visor_scene.h - seeded synthetic scenes for the Visor draw path.
+ *
+ * One generator, written in plain C, feeds every consumer of a scene: the CPU
+ * oracle, the reference build used to pin it, and the Vulkan-API driver that
+ * records the same scene into a command buffer for the GPU ICD.  All floating
+ * point inputs are produced in double precision with project-written
+ * deterministic math (no libm transcendental calls) and rounded to float32,
+ * so x86-64 and aarch64 hosts produce byte-identical scenes when compiled
+ * with -ffp-contract=off.
+ *
+ * A scene is a list of render passes.  Each pass targets one framebuffer
+ * (BGRA8 colour + D32 depth, the layout rasterizer.cpp:674-683 writes) and
+ * holds a contiguous run of draws.  Every draw names a pipeline (shader pair
+ * and fixed-function state), an optional texture and a range of the scene's
+ * single vertex/index buffer.
+ */
+#ifndef VISOR_SCENE_H
+#define VISOR_SCENE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Shader pairs the generator can emit (as SPIR-V through visor_spirv_emit). */
+enum {
+  VSC_SHADER_LAMBERT_TEX = 1,       /* pos/normal/uv; MVP push constant; tex * max(dot(N,L),0) */
+  VSC_SHADER_COLOR = 2,             /* clip-space pos + RGBA8 colour; colour pass-through */
+  VSC_SHADER_LAMBERT_TEX_ALPHA = 3, /* as LAMBERT_TEX plus a per-vertex alpha written to .w */
+};
+
+/* Vertex layouts implied by each shader (bytes per vertex). */
+#define VSC_STRIDE_LAMBERT_TEX 32u
+#define VSC_STRIDE_COLOR 20u
+#define VSC_STRIDE_LAMBERT_TEX_ALPHA 36u
+
+/* Texture filtering a pipeline's sampler asks for. */
+enum {
+  VSC_FILTER_REFERENCE = 0, /* bilinear, repeat, mip 0 only (texture_sampling.cpp:139-184) */
+  VSC_FILTER_TRILINEAR = 1, /* per-triangle analytic LOD, linear between two mips */
+  VSC_FILTER_NEAREST = 2,   /* nearest texel of mip 0, repeat */
+};
+
+/* Vulkan enum values used in the pipeline description (Vulkan 1.0 numbering). */
+enum {
+  VSC_CULL_NONE = 0, VSC_CULL_FRONT = 1, VSC_CULL_BACK = 2, VSC_CULL_FRONT_AND_BACK = 3,
+  VSC_FRONT_CCW = 0, VSC_FRONT_CW = 1,
+  VSC_CMP_NEVER = 0, VSC_CMP_LESS = 1, VSC_CMP_EQUAL = 2, VSC_CMP_LEQUAL = 3,
+  VSC_CMP_GREATER = 4, VSC_CMP_NOT_EQUAL = 5, VSC_CMP_GEQUAL = 6, VSC_CMP_ALWAYS = 7,
+  VSC_BLEND_ZERO = 0, VSC_BLEND_ONE = 1, VSC_BLEND_SRC_ALPHA = 6, VSC_BLEND_ONE_MINUS_SRC_ALPHA = 7,
+  VSC_TOPOLOGY_TRIANGLE_LIST = 3, VSC_TOPOLOGY_TRIANGLE_STRIP = 4,
+};
+
+typedef struct vsc_pipeline {
+  uint32_t shader;       /* VSC_SHADER_* */
+  uint32_t topology;     /* VSC_TOPOLOGY_* */
+  uint32_t cull_mode;    /* VSC_CULL_* */
+  uint32_t front_face;   /* VSC_FRONT_* */
+  uint32_t depth_test;   /* 0: no VkPipelineDepthStencilStateCreateInfo (compare ALWAYS) */
+  uint32_t depth_op;     /* VSC_CMP_* */
+  uint32_t depth_write;  /* 0/1 */
+  uint32_t blend_enable; /* 0/1 */
+  uint32_t src_factor;   /* VSC_BLEND_* */
+  uint32_t dst_factor;   /* VSC_BLEND_* */
+  uint32_t filter;       /* VSC_FILTER_* */
+} vsc_pipeline;
+
+typedef struct vsc_texture {
+  uint32_t width, height, mips;
+  uint64_t bytes;   /* all mips, packed as precompiled.cpp:3-36 lays them out */
+  uint8_t *texels;  /* RGBA8 */
+} vsc_texture;
+
+typedef struct vsc_target {
+  uint32_t width, height;
+} vsc_target;
+
+typedef struct vsc_draw {
+  uint32_t pipeline;  /* index into scene->pipelines */
+  uint32_t texture;   /* index into scene->textures, or VSC_NONE */
+  uint32_t indexed;   /* 1: vkCmdDrawIndexed, 0: vkCmdDraw */
+  uint32_t count;     /* index count (indexed) or vertex count */
+  uint32_t first;     /* first index or first vertex */
+  uint32_t push_size; /* bytes of push constants set before the draw */
+  uint64_t vb_offset; /* byte offset bound with vkCmdBindVertexBuffers */
+  uint8_t push[128];
+} vsc_draw;
+
+typedef struct vsc_pass {
+  uint32_t target;     /* index into scene->targets */
+  uint32_t clear;      /* loadOp CLEAR for colour and depth */
+  uint32_t first_draw; /* draws [first_draw, first_draw + draw_count) */
+  uint32_t draw_count;
+} vsc_pass;
+
+typedef struct vsc_scene {
+  uint32_t config;
+  uint64_t seed;
+  float clear_color[4];
+  float clear_depth;
+
+  uint32_t num_targets;
+  vsc_target *targets;
+  uint32_t num_pipelines;
+  vsc_pipeline *pipelines;
+  uint32_t num_textures;
+  vsc_texture *textures;
+
+  uint64_t vb_bytes; /* one vertex buffer shared by every draw */
+  uint8_t *vb;
+  uint64_t ib_count; /* one uint32 index buffer shared by every draw */
+  uint32_t *ib;
+
+  uint32_t num_draws;
+  vsc_draw *draws;
+  uint32_t num_passes;
+  vsc_pass *passes;
+
+  /* capacities (internal) */
+  uint32_t cap_targets, cap_pipelines, cap_textures, cap_draws, cap_passes;
+  uint64_t cap_vb, cap_ib;
+} vsc_scene;
+
+#define VSC_NONE 0xffffffffu
+
+/* Per-config overrides; 0 keeps the config's own value. */
+typedef struct vsc_params {
+  uint32_t width, height; /* target size */
+  uint32_t count;         /* cfg1 frames, cfg2 triangles, cfg3 draws, cfg4 targets, cfg5 requests */
+  uint32_t min_tris;      /* per-mesh triangle range (cfg3/4/5) */
+  uint32_t max_tris;
+  float max_area;         /* cfg2 largest triangle area in pixels */
+  uint32_t flags;         /* VSC_FLAG_* */
+  uint32_t textures;      /* number of distinct textures */
+  uint32_t tex_size;      /* texture edge */
+} vsc_params;
+
+enum {
+  VSC_FLAG_BACKFACE_CULL = 1u << 0, /* cull back faces instead of none */
+  VSC_FLAG_NO_BLEND = 1u << 1,      /* cfg2/cfg4: disable blending everywhere */
+  VSC_FLAG_FILTER_REFERENCE = 1u << 2, /* cfg3/5: sample mip 0 bilinearly like the reference */
+  VSC_FLAG_CLOCKWISE = 1u << 3,     /* front face clockwise */
+};
+
+/* Configurations of the headline workloads. */
+enum {
+  VSC_CFG_SPHERE = 1,    /* 512x512, UV sphere 64x32, bilinear texture, LESS, no blend */
+  VSC_CFG_TRIS = 2,      /* 1920x1080, 1M screen-space triangles, LEQUAL, alpha blend */
+  VSC_CFG_DRAWS = 3,     /* 2560x1440, 10k indexed draws, trilinear, LESS */
+  VSC_CFG_TARGETS = 4,   /* 1024 x 128x128 targets, half blended, bilinear */
+  VSC_CFG_SERVING = 5,   /* one serving request; count selects the request index */
+};
+
+/* Build a seeded scene.  Returns 0 on success. */
+int vsc_generate(uint32_t config, uint64_t seed, const vsc_params *params, vsc_scene **out);
+
+/* Manual construction, used by edge-case tests. */
+vsc_scene *vsc_new(void);
+void vsc_free(vsc_scene *s);
+uint32_t vsc_add_target(vsc_scene *s, uint32_t width, uint32_t height);
+uint32_t vsc_add_pipeline(vsc_scene *s, const vsc_pipeline *p);
+uint32_t vsc_add_texture(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
+                         const uint8_t *texels /* may be NULL: seeded random mip 0 */, uint64_t seed);
+uint64_t vsc_add_vertices(vsc_scene *s, const void *data, uint64_t bytes); /* returns byte offset */
+uint64_t vsc_add_indices(vsc_scene *s, const uint32_t *idx, uint64_t count); /* returns first index */
+uint32_t vsc_add_draw(vsc_scene *s, const vsc_draw *d);
+uint32_t vsc_add_pass(vsc_scene *s, uint32_t target, uint32_t clear, uint32_t first_draw,
+                      uint32_t draw_count);
+
+/* Vertex attribute layout each shader's pipeline declares (one binding, Vulkan format enums). */
+typedef struct vsc_attr {
+  uint32_t location;
+  uint32_t format; /* VkFormat: 37 R8G8B8A8_UNORM, 100 R32, 103 R32G32, 106 R32G32B32, 109 R32G32B32A32 SFLOAT */
+  uint32_t offset;
+} vsc_attr;
+
+/* Fills attrs (up to 4) and returns the attribute count for a shader. */
+uint32_t vsc_vertex_attrs(uint32_t shader, vsc_attr *attrs);
+
+/* Helpers the tests use to describe draws. */
+uint32_t vsc_stride_of(uint32_t shader);
+uint64_t vsc_texture_mip_offset(const vsc_texture *t, uint32_t mip);
+uint64_t vsc_triangle_count(const vsc_scene *s);
+uint64_t vsc_hash_bytes(const void *p, uint64_t n); /* FNV-1a 64 */
+
+/* Deterministic double math shared by the generator (no libm transcendental calls). */
+double vsc_sin(double x);
+double vsc_cos(double x);
+double vsc_exp(double x);
+double vsc_log(double x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

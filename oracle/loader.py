@@ -1,0 +1,122 @@
+"""Python access to the CPU oracle.  TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.  Two oracles are exposed:
+
+* `Oracle` - this project's C restatement (oracle/visor_oracle.c), built into
+  oracle/_build/liboracle.so on any host;
+* `Reference` - the reference's own draw path compiled from its sources into
+  oracle/_ref/libvisor_ref*.so by oracle/Makefile (only where the reference
+  tree is available).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from visor_gb300 import scene as vscene
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF = os.path.join(HERE, "_ref")
+COUNTER_NAMES = ("tris_in", "tris_out", "tested", "covered", "shaded", "draws")
+
+
+class Counters(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in COUNTER_NAMES]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n in COUNTER_NAMES}
+
+
+def build_oracle():
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+
+
+def build_reference(reference_dir):
+    subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFERENCE={reference_dir}"])
+
+
+class Oracle:
+    """The C restatement of the reference's draw path."""
+
+    def __init__(self, path=None):
+        path = path or os.path.join(BUILD, "liboracle.so")
+        if not os.path.exists(path):
+            build_oracle()
+        self.lib = vscene.bind_scene_api(C.CDLL(path))
+        SP = C.POINTER(vscene.Scene)
+        self.lib.vor_render.argtypes = [SP, C.c_void_p, C.c_void_p, C.POINTER(Counters)]
+        self.lib.vor_render.restype = C.c_int
+        self.lib.vor_render_passes.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                               C.POINTER(Counters)]
+        self.lib.vor_render_passes.restype = C.c_int
+        self.lib.vor_sample_bilinear.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
+                                                 C.c_float, C.POINTER(C.c_float)]
+        self.lib.vor_log2.argtypes = [C.c_float]
+        self.lib.vor_log2.restype = C.c_float
+
+    def generate(self, config, seed, **params):
+        return vscene.generate(self.lib, config, seed, **params)
+
+    def render(self, handle, passes=None):
+        cols, deps = vscene.target_buffers(handle)
+        cp, dp = vscene.pointer_arrays(cols, deps)
+        cnt = Counters()
+        if passes is None:
+            rc = self.lib.vor_render(handle.ptr, cp, dp, C.byref(cnt))
+        else:
+            rc = self.lib.vor_render_passes(handle.ptr, passes[0], passes[1], cp, dp, C.byref(cnt))
+        assert rc == 0
+        return cols, deps, cnt.as_dict()
+
+
+class Reference:
+    """The reference's own CPU draw path (built from its sources)."""
+
+    def __init__(self, fast=False):
+        path = os.path.join(REF, "libvisor_ref_fast.so" if fast else "libvisor_ref.so")
+        self.lib = vscene.bind_scene_api(C.CDLL(path))
+        SP = C.POINTER(vscene.Scene)
+        self.lib.visor_ref_render.argtypes = [SP, C.c_void_p, C.c_void_p,
+                                              C.POINTER(C.c_longlong), C.c_int,
+                                              C.POINTER(C.c_double)]
+        self.lib.visor_ref_render.restype = C.c_int
+        self.lib.visor_ref_time.argtypes = [SP, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        self.lib.visor_ref_time.restype = C.c_int
+
+    @staticmethod
+    def available():
+        return os.path.exists(os.path.join(REF, "libvisor_ref.so"))
+
+    def render(self, handle, threaded=False):
+        cols, deps = vscene.target_buffers(handle)
+        cp, dp = vscene.pointer_arrays(cols, deps)
+        cnt = (C.c_longlong * 6)()
+        secs = C.c_double()
+        rc = self.lib.visor_ref_render(handle.ptr, cp, dp, cnt, 1 if threaded else 0, C.byref(secs))
+        assert rc == 0, rc
+        counters = {n: int(cnt[i]) for i, n in enumerate(COUNTER_NAMES)}
+        return cols, deps, counters, secs.value
+
+    def time(self, handle, threaded, steps):
+        out = (C.c_double * steps)()
+        rc = self.lib.visor_ref_time(handle.ptr, 1 if threaded else 0, steps, out)
+        assert rc == 0, rc
+        return list(out)
+
+
+def frame_hash(cols, deps):
+    """FNV-1a-64 over every target's colour then depth bytes (stable fixture key)."""
+    h = 0xCBF29CE484222325
+    for c, d in zip(cols, deps):
+        for arr in (c, d):
+            b = np.ascontiguousarray(arr).view(np.uint8).ravel()
+            # vectorised FNV is not possible; hash the per-target digest instead
+            import hashlib
+            dig = hashlib.sha256(b.tobytes()).digest()
+            for byte in dig:
+                h ^= byte
+                h = (h * 0x100000001B3) & 0xFFFFFFFFFFFFFFFF
+    return f"{h:016x}"

@@ -1,0 +1,752 @@
+/*
+ * visor_oracle.c - CPU restatement of Visor's draw path.  TEST INFRASTRUCTURE.
+ *
+ * Only tests, the smoke check and bench.py's CPU-baseline leg use this file;
+ * the product never links it.  Each function restates a reference function,
+ * named with its file:line in baldurk/visor.  Arithmetic follows the
+ * reference's operation order exactly (binary32, round to nearest, no FMA:
+ * build with -ffp-contract=off), so results are bit-identical to the
+ * reference rasterizer built from its own sources (oracle/_ref).
+ *
+ * Parity status: pinned against oracle/_ref for everything the reference
+ * implements (bilinear mip-0 sampling, coverage, depth, blend, counters).
+ * Trilinear and nearest filtering have no reference implementation; their
+ * functions below are this project's specification ("parity unpinned").
+ */
+#include "visor_oracle.h"
+
+#include <limits.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef struct f4 {
+  float v[4];
+} f4;
+
+/* VertexCacheEntry, gpu.h:53-57 */
+typedef struct vcache {
+  f4 position;
+  f4 interps[10];
+} vcache;
+
+typedef struct draw_ctx {
+  const vsc_scene *s;
+  const vsc_draw *d;
+  const vsc_pipeline *p;
+  const vsc_texture *tex;
+  vsc_attr attrs[4];
+  uint32_t nattrs;
+  uint32_t stride;
+  const uint8_t *vb;
+  const uint32_t *ib;
+  uint32_t w, h;
+  uint8_t *col;
+  float *depth;
+  vor_counters *cnt;
+} draw_ctx;
+
+typedef struct tri_ctx {
+  const vcache *v; /* the triangle's three VS outputs */
+  float lod;       /* trilinear LOD (project specification) */
+} tri_ctx;
+
+/* ------------------------------------------------------------------------ */
+/* shader runtime helpers                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* GetVertexAttributeData, spirv_compile.cpp:572-627 */
+static f4 fetch_attr(const draw_ctx *c, uint32_t loc, uint32_t index)
+{
+  f4 out = {{0.0f, 0.0f, 0.0f, 1.0f}};
+  const vsc_attr *a = NULL;
+  for(uint32_t i = 0; i < c->nattrs; i++)
+    if(c->attrs[i].location == loc)
+      a = &c->attrs[i];
+  if(!a)
+    return out;
+  const uint8_t *ptr = c->vb + a->offset + (uint64_t)c->stride * index;
+  float f[4];
+  uint32_t u;
+  switch(a->format)
+  {
+    case 109: memcpy(f, ptr, 16); out.v[3] = f[3]; /* fall through */
+    case 106: memcpy(f, ptr, 12); out.v[2] = f[2]; /* fall through */
+    case 103: memcpy(f, ptr, 8); out.v[1] = f[1];  /* fall through */
+    case 100: memcpy(f, ptr, 4); out.v[0] = f[0]; break;
+    case 37:
+      memcpy(&u, ptr, 4);
+      out.v[0] = (float)((u & 0x000000ffu) >> 0) / 255.0f;
+      out.v[1] = (float)((u & 0x0000ff00u) >> 8) / 255.0f;
+      out.v[2] = (float)((u & 0x00ff0000u) >> 16) / 255.0f;
+      out.v[3] = (float)((u & 0xff000000u) >> 24) / 255.0f;
+      break;
+    default: break;
+  }
+  return out;
+}
+
+/* Float4x4TimesVec4, spirv_compile.cpp:423-431 (column-major fmat[col*4+row]) */
+static f4 mat4_times_vec4(const float *m, f4 v)
+{
+  f4 out;
+  for(int row = 0; row < 4; row++)
+  {
+    out.v[row] = 0.0f;
+    for(int col = 0; col < 4; col++)
+      out.v[row] = out.v[row] + m[col * 4 + row] * v.v[col];
+  }
+  return out;
+}
+
+/*
+ * Fragment input interpolation: the FS wrapper dots the barycentrics with the
+ * component taken from each vertex (spirv_compile.cpp:2200-2214) using
+ * CreateDot (:629-643) over four lanes whose last lane is bary.w * 0.
+ */
+static float interp(f4 bary, float a, float b, float c)
+{
+  float acc = bary.v[0] * a;
+  acc = acc + bary.v[1] * b;
+  acc = acc + bary.v[2] * c;
+  acc = acc + bary.v[3] * 0.0f;
+  return acc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* texture sampling                                                          */
+/* ------------------------------------------------------------------------ */
+
+static f4 texel(const uint8_t *base, uint32_t width, int x, int y)
+{
+  /* CacheCoord fills its cache with float(byte)/255.0f per channel, texture_sampling.cpp:123-133 */
+  const uint8_t *p = base + ((uint64_t)y * width + (uint32_t)x) * 4;
+  f4 t;
+  for(int ch = 0; ch < 4; ch++)
+    t.v[ch] = (float)p[ch] / 255.0f;
+  return t;
+}
+
+/* sample_tex_wrapped, texture_sampling.cpp:139-184 */
+void vor_sample_bilinear(const uint8_t *texels, uint32_t width, uint32_t height, float u, float v,
+                         float out[4])
+{
+  u = u - floorf(u);
+  v = v - floorf(v);
+
+  u = u * (float)width;
+  v = v * (float)height;
+
+  int iu0 = (int)u;
+  int iv0 = (int)v;
+  int iu1 = iu0 + 1;
+  int iv1 = iv0 + 1;
+
+  if(iu1 >= (int)width)
+    iu1 -= width;
+  if(iv1 >= (int)height)
+    iv1 -= height;
+
+  float fu = u - (float)iu0;
+  float fv = v - (float)iv0;
+  float inv_fu = 1.0f - fu;
+  float inv_fv = 1.0f - fv;
+
+  /* u - floor(u) can round to 1.0f for tiny negative u; the reference then
+     reads past the row.  The specification wraps that texel instead. */
+  if(iu0 >= (int)width)
+    iu0 -= width;
+  if(iv0 >= (int)height)
+    iv0 -= height;
+
+  f4 TL = texel(texels, width, iu0, iv0);
+  f4 TR = texel(texels, width, iu1, iv0);
+  f4 BL = texel(texels, width, iu0, iv1);
+  f4 BR = texel(texels, width, iu1, iv1);
+
+  for(int ch = 0; ch < 4; ch++)
+  {
+    float top = TL.v[ch] * inv_fu + TR.v[ch] * fu;
+    float bottom = BL.v[ch] * inv_fu + BR.v[ch] * fu;
+    out[ch] = top * inv_fv + bottom * fv;
+  }
+}
+
+/*
+ * Project specification (no reference counterpart): log2 for the trilinear
+ * LOD from the exponent bits and the series 2/ln2 * (s + s^3/3 + s^5/5),
+ * s = (m-1)/(m+1), evaluated in this exact order on CPU and GPU.
+ */
+float vor_log2(float x)
+{
+  if(!(x > 0.0f))
+    return -128.0f;
+  if(x > 3.0e38f)
+    return 128.0f;
+  uint32_t bits;
+  memcpy(&bits, &x, 4);
+  int e = (int)((bits >> 23) & 0xffu) - 127;
+  uint32_t mb = (bits & 0x007fffffu) | 0x3f800000u;
+  float m;
+  memcpy(&m, &mb, 4);
+  float s = (m - 1.0f) / (m + 1.0f);
+  float s2 = s * s;
+  float poly = s + s * s2 * (1.0f / 3.0f) + s * s2 * s2 * 0.2f;
+  return (float)e + poly * 2.88539008f;
+}
+
+/*
+ * Project specification: per-triangle LOD = 0.5*log2(texel area / pixel area)
+ * with the texel area from the triangle's uv at mip 0 and the pixel area from
+ * the integer doubled area of the setup (rasterizer.cpp:272-275).
+ */
+float vor_lod(float u0, float v0, float u1, float v1, float u2, float v2, uint32_t width,
+              uint32_t height, int area2)
+{
+  float du1 = u1 - u0, dv1 = v1 - v0, du2 = u2 - u0, dv2 = v2 - v0;
+  float cr = du1 * dv2 - du2 * dv1;
+  float auv = fabsf(cr) * (float)width * (float)height;
+  float apx = (float)(area2 < 0 ? -area2 : area2);
+  return 0.5f * vor_log2(auv / apx);
+}
+
+/* Project specification: bilinear on mip floor(lod) and the next, blended by frac(lod). */
+void vor_sample_trilinear(const vsc_texture *tex, float lod, float u, float v, float out[4])
+{
+  float maxl = (float)(tex->mips - 1);
+  if(!(lod > 0.0f))
+    lod = 0.0f;
+  if(lod > maxl)
+    lod = maxl;
+  int l0 = (int)lod;
+  float f = lod - (float)l0;
+  int l1 = l0 + 1 < (int)tex->mips ? l0 + 1 : l0;
+  uint32_t w0 = tex->width >> l0, h0 = tex->height >> l0;
+  if(w0 < 1) w0 = 1;
+  if(h0 < 1) h0 = 1;
+  float c0[4];
+  vor_sample_bilinear(tex->texels + vsc_texture_mip_offset(tex, l0), w0, h0, u, v, c0);
+  if(f > 0.0f)
+  {
+    uint32_t w1 = tex->width >> l1, h1 = tex->height >> l1;
+    if(w1 < 1) w1 = 1;
+    if(h1 < 1) h1 = 1;
+    float c1[4];
+    vor_sample_bilinear(tex->texels + vsc_texture_mip_offset(tex, l1), w1, h1, u, v, c1);
+    float g = 1.0f - f;
+    for(int ch = 0; ch < 4; ch++)
+      out[ch] = c0[ch] * g + c1[ch] * f;
+  }
+  else
+  {
+    for(int ch = 0; ch < 4; ch++)
+      out[ch] = c0[ch];
+  }
+}
+
+/* Project specification: nearest texel of mip 0 with repeat addressing. */
+static void sample_nearest(const vsc_texture *tex, float u, float v, float out[4])
+{
+  u = u - floorf(u);
+  v = v - floorf(v);
+  int iu = (int)(u * (float)tex->width);
+  int iv = (int)(v * (float)tex->height);
+  if(iu >= (int)tex->width)
+    iu -= tex->width;
+  if(iv >= (int)tex->height)
+    iv -= tex->height;
+  f4 t = texel(tex->texels, tex->width, iu, iv);
+  for(int ch = 0; ch < 4; ch++)
+    out[ch] = t.v[ch];
+}
+
+/* OpImageSampleImplicitLod lowering, spirv_compile.cpp:1842-1886 (byte offset 0 = mip 0). */
+static f4 sample(const draw_ctx *c, const tri_ctx *t, float u, float v)
+{
+  f4 r = {{0.0f, 0.0f, 0.0f, 0.0f}};
+  if(!c->tex)
+    return r;
+  switch(c->p->filter)
+  {
+    case VSC_FILTER_TRILINEAR: vor_sample_trilinear(c->tex, t->lod, u, v, r.v); break;
+    case VSC_FILTER_NEAREST: sample_nearest(c->tex, u, v, r.v); break;
+    default: vor_sample_bilinear(c->tex->texels, c->tex->width, c->tex->height, u, v, r.v); break;
+  }
+  return r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* the configurations' shaders, in the reference JIT's lowering order        */
+/* ------------------------------------------------------------------------ */
+
+static void push_floats(const draw_ctx *c, uint32_t offset, float *dst, uint32_t n)
+{
+  /* GetPushConstantPointer, spirv_compile.cpp:566-570 */
+  memcpy(dst, c->d->push + offset, n * 4);
+}
+
+/*
+ * VS: gl_Position = mvp * vec4(pos, 1.0); out0 = normal; out1 = uv; [out2 = alpha].
+ * Inputs truncate the fetched float4 (spirv_compile.cpp:1957-1992); outputs of
+ * fewer than four components are padded with component 0 (:2057-2065).
+ */
+static void vs_lambert(const draw_ctx *c, uint32_t index, vcache *out, int with_alpha)
+{
+  float mvp[16];
+  push_floats(c, 0, mvp, 16);
+  f4 pos = fetch_attr(c, 0, index);
+  f4 nrm = fetch_attr(c, 1, index);
+  f4 uv = fetch_attr(c, 2, index);
+  f4 p4 = {{pos.v[0], pos.v[1], pos.v[2], 1.0f}};
+  out->position = mat4_times_vec4(mvp, p4);
+  f4 o0 = {{nrm.v[0], nrm.v[1], nrm.v[2], nrm.v[0]}};
+  f4 o1 = {{uv.v[0], uv.v[1], uv.v[0], uv.v[0]}};
+  out->interps[0] = o0;
+  out->interps[1] = o1;
+  if(with_alpha)
+  {
+    f4 al = fetch_attr(c, 3, index);
+    f4 o2 = {{al.v[0], al.v[0], al.v[0], al.v[0]}}; /* scalar outputs are splatted (:2066-2069) */
+    out->interps[2] = o2;
+  }
+}
+
+/* VS: gl_Position = pos; out0 = colour (RGBA8 UNORM decoded by the fetch). */
+static void vs_color(const draw_ctx *c, uint32_t index, vcache *out)
+{
+  out->position = fetch_attr(c, 0, index);
+  out->interps[0] = fetch_attr(c, 1, index);
+}
+
+/*
+ * FS: n = normalize(in0); l = max(dot(n, light.xyz), 0); t = texture(tex, in1);
+ * colour = t * l  [or vec4(t.xyz * l, in2) with alpha].
+ * Normalize = a * (1/sqrt(dot(a,a))) (spirv_compile.cpp:1635-1647), dot is
+ * CreateDot (:629-643), FMax is select(a > b, a, b) (:1535-1545),
+ * vector*scalar is a per-lane multiply (:1470-1476).
+ */
+static f4 fs_lambert(const draw_ctx *c, const tri_ctx *t, f4 bary, int with_alpha)
+{
+  const vcache *v = t->v;
+  float n[3], uv[2], light[4];
+  for(int i = 0; i < 3; i++)
+    n[i] = interp(bary, v[0].interps[0].v[i], v[1].interps[0].v[i], v[2].interps[0].v[i]);
+  for(int i = 0; i < 2; i++)
+    uv[i] = interp(bary, v[0].interps[1].v[i], v[1].interps[1].v[i], v[2].interps[1].v[i]);
+
+  float sq = n[0] * n[0];
+  sq = sq + n[1] * n[1];
+  sq = sq + n[2] * n[2];
+  float len = sqrtf(sq);
+  float inv = 1.0f / len;
+  float nn[3] = {n[0] * inv, n[1] * inv, n[2] * inv};
+
+  push_floats(c, 64, light, 4);
+  float d = nn[0] * light[0];
+  d = d + nn[1] * light[1];
+  d = d + nn[2] * light[2];
+  float lam = d > 0.0f ? d : 0.0f;
+
+  f4 tex = sample(c, t, uv[0], uv[1]);
+  f4 out;
+  if(!with_alpha)
+  {
+    for(int i = 0; i < 4; i++)
+      out.v[i] = tex.v[i] * lam;
+  }
+  else
+  {
+    for(int i = 0; i < 3; i++)
+      out.v[i] = tex.v[i] * lam;
+    out.v[3] = interp(bary, v[0].interps[2].v[0], v[1].interps[2].v[0], v[2].interps[2].v[0]);
+  }
+  return out;
+}
+
+static f4 fs_color(const tri_ctx *t, f4 bary)
+{
+  const vcache *v = t->v;
+  f4 out;
+  for(int i = 0; i < 4; i++)
+    out.v[i] = interp(bary, v[0].interps[0].v[i], v[1].interps[0].v[i], v[2].interps[0].v[i]);
+  return out;
+}
+
+static void run_vs(const draw_ctx *c, uint32_t index, vcache *out)
+{
+  memset(out, 0, sizeof(*out));
+  switch(c->p->shader)
+  {
+    case VSC_SHADER_LAMBERT_TEX: vs_lambert(c, index, out, 0); break;
+    case VSC_SHADER_LAMBERT_TEX_ALPHA: vs_lambert(c, index, out, 1); break;
+    case VSC_SHADER_COLOR: vs_color(c, index, out); break;
+    default: break;
+  }
+}
+
+static f4 run_fs(const draw_ctx *c, const tri_ctx *t, f4 bary)
+{
+  switch(c->p->shader)
+  {
+    case VSC_SHADER_LAMBERT_TEX: return fs_lambert(c, t, bary, 0);
+    case VSC_SHADER_LAMBERT_TEX_ALPHA: return fs_lambert(c, t, bary, 1);
+    case VSC_SHADER_COLOR: return fs_color(t, bary);
+    default:
+    {
+      f4 z = {{0, 0, 0, 0}};
+      return z;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* fixed function                                                            */
+/* ------------------------------------------------------------------------ */
+
+/* ClearTarget (colour), rasterizer.cpp:332-361: truncating byte(f*255), BGRA order. */
+static void clear_color(uint8_t *bits, uint32_t w, uint32_t h, const float *col)
+{
+  uint8_t e[4];
+  e[2] = (uint8_t)(col[0] * 255.0f);
+  e[1] = (uint8_t)(col[1] * 255.0f);
+  e[0] = (uint8_t)(col[2] * 255.0f);
+  e[3] = (uint8_t)(col[3] * 255.0f);
+  for(uint64_t i = 0; i < (uint64_t)w * h; i++)
+    memcpy(bits + i * 4, e, 4);
+}
+
+/* ClearTarget (depth), rasterizer.cpp:312-330 */
+static void clear_depth(float *d, uint32_t w, uint32_t h, float v)
+{
+  for(uint64_t i = 0; i < (uint64_t)w * h; i++)
+    d[i] = v;
+}
+
+/* GetIndex, rasterizer.cpp:100-119 (uint32 indices) */
+static uint32_t get_index(const draw_ctx *c, uint32_t vertexIndex)
+{
+  if(!c->d->indexed)
+    return vertexIndex;
+  return c->ib[vertexIndex];
+}
+
+/* clamp01, rasterizer.cpp:277-280 */
+static float clamp01(float in) { return in > 1.0f ? 1.0f : (in < 0.0f ? 0.0f : in); }
+
+/* ShadeVerts, rasterizer.cpp:121-237: 3 VS invocations per triangle, strips re-use. */
+static uint64_t shade_verts(const draw_ctx *c, vcache **out)
+{
+  uint32_t num = c->d->count, first = c->d->first;
+  uint64_t ntris = 0;
+  if(c->p->topology == VSC_TOPOLOGY_TRIANGLE_STRIP)
+    ntris = num >= 3 ? num - 2 : 0;
+  else
+    ntris = num / 3;
+  vcache *v = (vcache *)malloc((size_t)(ntris ? ntris : 1) * 3 * sizeof(vcache));
+  uint64_t k = 0;
+  if(c->p->topology == VSC_TOPOLOGY_TRIANGLE_STRIP)
+  {
+    if(num >= 3)
+    {
+      vcache tri[4];
+      uint32_t vi = first;
+      int remaining = (int)num;
+      run_vs(c, get_index(c, vi++), &tri[0]);
+      run_vs(c, get_index(c, vi++), &tri[1]);
+      run_vs(c, get_index(c, vi++), &tri[2]);
+      v[k++] = tri[0];
+      v[k++] = tri[1];
+      v[k++] = tri[2];
+      remaining -= 3;
+      if(remaining > 0)
+      {
+        run_vs(c, get_index(c, vi++), &tri[3]);
+        remaining--;
+        v[k++] = tri[2];
+        v[k++] = tri[1];
+        v[k++] = tri[3];
+      }
+      while(remaining > 0)
+      {
+        tri[0] = tri[2];
+        tri[1] = tri[3];
+        run_vs(c, get_index(c, vi++), &tri[2]);
+        remaining--;
+        v[k++] = tri[0];
+        v[k++] = tri[1];
+        v[k++] = tri[2];
+        if(remaining > 0)
+        {
+          run_vs(c, get_index(c, vi++), &tri[3]);
+          remaining--;
+          v[k++] = tri[2];
+          v[k++] = tri[1];
+          v[k++] = tri[3];
+        }
+      }
+    }
+  }
+  else
+  {
+    uint32_t vi = first;
+    for(uint64_t t = 0; t < ntris; t++)
+    {
+      run_vs(c, get_index(c, vi++), &v[k++]);
+      run_vs(c, get_index(c, vi++), &v[k++]);
+      run_vs(c, get_index(c, vi++), &v[k++]);
+    }
+  }
+  *out = v;
+  return k / 3;
+}
+
+/* ToWindow, rasterizer.cpp:239-253: truncation toward zero, no subpixel bits. */
+static void to_window(uint32_t w, uint32_t h, const f4 *p, int *x, int *y)
+{
+  *x = (int)((p->v[0] / p->v[3] + 1.0f) * 0.5f * (float)w);
+  *y = (int)((p->v[1] * -1.0f / p->v[3] + 1.0f) * 0.5f * (float)h);
+}
+
+/* Per-pixel work of ProcessTriangles, rasterizer.cpp:538-691. */
+static void process_triangle(const draw_ctx *c, const tri_ctx *t, const int *wx, const int *wy,
+                             int area2, int barymul, float invarea, const float *invw,
+                             const float *depth, int minx, int miny, int maxx, int maxy)
+{
+  const vsc_pipeline *p = c->p;
+  const uint32_t w = c->w;
+  uint8_t *bits = c->col;
+  float *depthbits = c->depth;
+  const int ABx = wx[1] - wx[0], ABy = wy[1] - wy[0];
+  const int ACx = wx[2] - wx[0], ACy = wy[2] - wy[0];
+  uint32_t depth_op = p->depth_test ? p->depth_op : VSC_CMP_ALWAYS;
+  uint64_t written = 0, tested = 0, passed_n = 0;
+
+  for(int y = miny; y < maxy; y++)
+  {
+    for(int x = minx; x < maxx; x++)
+    {
+      /* barycentric, rasterizer.cpp:282-310 */
+      const int PAx = wx[0] - x;
+      const int PAy = wy[0] - y;
+      const int ux = (ACx * PAy) - (ACy * PAx);
+      const int uy = (PAx * ABy) - (PAy * ABx);
+      int b0 = (area2 - (ux + uy)) * barymul;
+      int b1 = ux * barymul;
+      int b2 = uy * barymul;
+
+      if(b0 >= 0 && b1 >= 0 && b2 >= 0)
+      {
+        f4 n = {{(float)b0, (float)b1, (float)b2, 0.0f}};
+        n.v[0] = n.v[0] * invarea;
+        n.v[1] = n.v[1] * invarea;
+        n.v[2] = n.v[2] * invarea;
+
+        float pixdepth = n.v[0] * depth[0] + n.v[1] * depth[1] + n.v[2] * depth[2];
+
+        int passed = 1;
+        uint64_t pix = (uint64_t)y * w + (uint64_t)x;
+        if(depth_op != VSC_CMP_ALWAYS && depthbits)
+        {
+          float cur = depthbits[pix];
+          switch(depth_op)
+          {
+            case VSC_CMP_NEVER: passed = 0; break;
+            case VSC_CMP_LESS: passed = pixdepth < cur; break;
+            case VSC_CMP_EQUAL: passed = pixdepth == cur; break;
+            case VSC_CMP_LEQUAL: passed = pixdepth <= cur; break;
+            case VSC_CMP_GREATER: passed = pixdepth > cur; break;
+            case VSC_CMP_NOT_EQUAL: passed = pixdepth != cur; break;
+            case VSC_CMP_GEQUAL: passed = pixdepth >= cur; break;
+          }
+        }
+
+        if(passed)
+        {
+          /* perspective correction, rasterizer.cpp:580-588 */
+          n.v[0] = n.v[0] * invw[0];
+          n.v[1] = n.v[1] * invw[1];
+          n.v[2] = n.v[2] * invw[2];
+          float invlen = 1.0f / (n.v[0] + n.v[1] + n.v[2]);
+          n.v[0] = n.v[0] * invlen;
+          n.v[1] = n.v[1] * invlen;
+          n.v[2] = n.v[2] * invlen;
+
+          f4 pixc = run_fs(c, t, n);
+
+          if(p->blend_enable)
+          {
+            /* rasterizer.cpp:593-672: destination alpha reads as 1.0 */
+            float ex[4] = {(float)bits[pix * 4 + 2], (float)bits[pix * 4 + 1],
+                           (float)bits[pix * 4 + 0], 1.0f};
+            ex[0] = ex[0] / 255.0f;
+            ex[1] = ex[1] / 255.0f;
+            ex[2] = ex[2] / 255.0f;
+            float sf = 1.0f, df = 1.0f;
+            switch(p->src_factor)
+            {
+              case VSC_BLEND_ZERO: sf = 0.0f; break;
+              case VSC_BLEND_ONE: sf = 1.0f; break;
+              case VSC_BLEND_SRC_ALPHA: sf = pixc.v[3]; break;
+              case VSC_BLEND_ONE_MINUS_SRC_ALPHA: sf = 1.0f - pixc.v[3]; break;
+              default: break;
+            }
+            switch(p->dst_factor)
+            {
+              case VSC_BLEND_ZERO: df = 0.0f; break;
+              case VSC_BLEND_ONE: df = 1.0f; break;
+              case VSC_BLEND_SRC_ALPHA: df = pixc.v[3]; break;
+              case VSC_BLEND_ONE_MINUS_SRC_ALPHA: df = 1.0f - pixc.v[3]; break;
+              default: break;
+            }
+            f4 bl;
+            for(int i = 0; i < 4; i++)
+              bl.v[i] = sf * pixc.v[i] + df * ex[i];
+            pixc = bl;
+          }
+
+          /* rasterizer.cpp:674-676: R,G,B to bytes 2,1,0; alpha byte untouched */
+          bits[pix * 4 + 2] = (uint8_t)(clamp01(pixc.v[0]) * 255.0f);
+          bits[pix * 4 + 1] = (uint8_t)(clamp01(pixc.v[1]) * 255.0f);
+          bits[pix * 4 + 0] = (uint8_t)(clamp01(pixc.v[2]) * 255.0f);
+
+          passed_n++;
+
+          if(p->depth_write && p->depth_test && depthbits)
+            depthbits[pix] = pixdepth;
+        }
+        written++;
+      }
+      tested++;
+    }
+  }
+  c->cnt->tested += tested;
+  c->cnt->covered += written;
+  c->cnt->shaded += passed_n;
+}
+
+/* DrawTriangles, rasterizer.cpp:363-520, serial FIFO order. */
+static void draw_triangles(draw_ctx *c)
+{
+  vcache *vs = NULL;
+  uint64_t ntris = shade_verts(c, &vs);
+  const int w = (int)c->w, h = (int)c->h;
+
+  for(uint64_t t = 0; t < ntris; t++)
+  {
+    const vcache *v = &vs[t * 3];
+    int wx[3], wy[3];
+    for(int k = 0; k < 3; k++)
+      to_window(c->w, c->h, &v[k].position, &wx[k], &wy[k]);
+
+    c->cnt->tris_in++;
+
+    /* double_triarea, rasterizer.cpp:272-275 */
+    int area2 = (wx[1] - wx[0]) * (wy[2] - wy[0]) - (wy[1] - wy[0]) * (wx[2] - wx[0]);
+    if(area2 == 0)
+      continue;
+
+    int area2_flipped = area2;
+    int barymul = 1;
+    if(c->p->front_face == VSC_FRONT_CW)
+    {
+      barymul *= -1;
+      area2_flipped *= -1;
+    }
+    if(area2_flipped > 0 && (c->p->cull_mode & VSC_CULL_FRONT))
+      continue;
+    if(area2_flipped < 0)
+    {
+      if(c->p->cull_mode & VSC_CULL_BACK)
+        continue;
+      barymul *= -1;
+      area2_flipped *= -1;
+    }
+
+    c->cnt->tris_out++;
+
+    /* MinMax + clamp, rasterizer.cpp:428-435 */
+    int minx = INT_MAX, miny = INT_MAX, maxx = INT_MIN, maxy = INT_MIN;
+    for(int k = 0; k < 3; k++)
+    {
+      minx = wx[k] < minx ? wx[k] : minx;
+      miny = wy[k] < miny ? wy[k] : miny;
+      maxx = wx[k] > maxx ? wx[k] : maxx;
+      maxy = wy[k] > maxy ? wy[k] : maxy;
+    }
+    minx = minx > 0 ? minx : 0;
+    miny = miny > 0 ? miny : 0;
+    maxx = maxx < w - 1 ? maxx : w - 1;
+    maxy = maxy < h - 1 ? maxy : h - 1;
+
+    /* TriangleWork setup, rasterizer.cpp:437-452 */
+    float invarea = 1.0f / (float)area2_flipped;
+    float invw[3], depth[3];
+    for(int k = 0; k < 3; k++)
+    {
+      invw[k] = 1.0f / v[k].position.v[3];
+      depth[k] = v[k].position.v[2] * invw[k];
+    }
+
+    tri_ctx tc;
+    tc.v = v;
+    tc.lod = 0.0f;
+    if(c->p->filter == VSC_FILTER_TRILINEAR && c->tex)
+      tc.lod = vor_lod(v[0].interps[1].v[0], v[0].interps[1].v[1], v[1].interps[1].v[0],
+                       v[1].interps[1].v[1], v[2].interps[1].v[0], v[2].interps[1].v[1],
+                       c->tex->width, c->tex->height, area2);
+
+    /* The 32x32 block split (:454-480) partitions [min,max) exactly; FIFO
+       draining processes the blocks of one triangle before the next. */
+    process_triangle(c, &tc, wx, wy, area2, barymul, invarea, invw, depth, minx, miny, maxx,
+                     maxy);
+  }
+  c->cnt->draws++;
+  free(vs);
+}
+
+int vor_render_passes(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
+                      float **depths, vor_counters *counters)
+{
+  vor_counters local;
+  memset(&local, 0, sizeof(local));
+  for(uint32_t pi = first; pi < first + count && pi < s->num_passes; pi++)
+  {
+    const vsc_pass *pass = &s->passes[pi];
+    const vsc_target *tg = &s->targets[pass->target];
+    uint8_t *col = colors[pass->target];
+    float *dep = depths[pass->target];
+    /* BeginRenderPass, cmd_exec.cpp:35-64 */
+    if(pass->clear)
+    {
+      clear_color(col, tg->width, tg->height, s->clear_color);
+      clear_depth(dep, tg->width, tg->height, s->clear_depth);
+    }
+    for(uint32_t di = pass->first_draw; di < pass->first_draw + pass->draw_count; di++)
+    {
+      draw_ctx c;
+      memset(&c, 0, sizeof(c));
+      c.s = s;
+      c.d = &s->draws[di];
+      c.p = &s->pipelines[c.d->pipeline];
+      c.tex = c.d->texture != VSC_NONE ? &s->textures[c.d->texture] : NULL;
+      c.nattrs = vsc_vertex_attrs(c.p->shader, c.attrs);
+      c.stride = vsc_stride_of(c.p->shader);
+      c.vb = s->vb + c.d->vb_offset;
+      c.ib = s->ib;
+      c.w = tg->width;
+      c.h = tg->height;
+      c.col = col;
+      c.depth = dep;
+      c.cnt = &local;
+      draw_triangles(&c);
+    }
+  }
+  if(counters)
+    *counters = local;
+  return 0;
+}
+
+int vor_render(const vsc_scene *s, uint8_t **colors, float **depths, vor_counters *counters)
+{
+  return vor_render_passes(s, 0, s->num_passes, colors, depths, counters);
+}

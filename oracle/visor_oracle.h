@@ -1,0 +1,60 @@
+/*
+ * visor_oracle.h - CPU restatement of Visor's draw path.  TEST INFRASTRUCTURE.
+ *
+ * This is the oracle the GPU path is checked against.  It is NOT part of the
+ * product: only tests, the smoke check and the CPU-baseline leg of bench.py
+ * may load it.  Every function restates one function of the reference
+ * (baldurk/visor) and cites the file:line it follows.  Parity is pinned by
+ * comparing this restatement with the reference's own rasterizer sources,
+ * built unmodified by oracle/Makefile into oracle/_ref, on seeded scenes;
+ * tests/golden holds the fixtures that comparison produced.
+ *
+ * Execution model: the reference's serial FIFO mode (no worker threads,
+ * rasterizer.cpp:488-515 drains blocks in primitive order on the submitting
+ * thread), i.e. every pixel sees its triangles in primitive order.
+ */
+#ifndef VISOR_ORACLE_H
+#define VISOR_ORACLE_H
+
+#include <stdint.h>
+
+#include "visor_scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The reference's microprofile counters (rasterizer.cpp:517-519, 693-695). */
+typedef struct vor_counters {
+  uint64_t tris_in;  /* rasterizer/triangles/in */
+  uint64_t tris_out; /* rasterizer/triangles/out */
+  uint64_t tested;   /* rasterizer/pixels/tested */
+  uint64_t covered;  /* rasterizer/pixels/written */
+  uint64_t shaded;   /* rasterizer/depth/passed */
+  uint64_t draws;    /* rasterizer/draws/in */
+} vor_counters;
+
+/*
+ * Render every pass of the scene.  colors[t] (width*height*4 bytes, BGRA) and
+ * depths[t] (width*height floats) receive target t; they need not be
+ * initialised when the target's pass clears.  Returns 0 on success.
+ */
+int vor_render(const vsc_scene *scene, uint8_t **colors, float **depths, vor_counters *counters);
+
+/* Render only passes [first, first + count) (used for bounded CPU timing samples). */
+int vor_render_passes(const vsc_scene *scene, uint32_t first, uint32_t count, uint8_t **colors,
+                      float **depths, vor_counters *counters);
+
+/* Texture sampling entry points, exposed for unit tests. */
+void vor_sample_bilinear(const uint8_t *texels, uint32_t width, uint32_t height, float u, float v,
+                         float out[4]);
+void vor_sample_trilinear(const vsc_texture *tex, float lod, float u, float v, float out[4]);
+float vor_lod(float u0, float v0, float u1, float v1, float u2, float v2, uint32_t width,
+              uint32_t height, int area2);
+float vor_log2(float x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

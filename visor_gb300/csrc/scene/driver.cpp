@@ -1,0 +1,783 @@
+/*
+ * Records a vsc_scene through the Vulkan API of an ICD (see include/visor_driver.h).
+ *
+ * Compiled twice: against include/visor_vk.h for this project's ICD, and
+ * against the reference's Khronos header (VISOR_DRIVER_KHRONOS_HEADER) for the
+ * reference ICD built as an oracle.  Only Vulkan 1.0 names are used.
+ */
+#ifdef VISOR_DRIVER_KHRONOS_HEADER
+#include "3rdparty/vulkan.h"
+#else
+#include "visor_vk.h"
+#endif
+
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "visor_driver.h"
+#include "visor_spirv.h"
+
+namespace
+{
+struct Fns
+{
+#define VSD_FN(name) PFN_##name name = nullptr;
+#define VSD_FNS(X)                                                                            \
+  X(vkCreateInstance) X(vkDestroyInstance) X(vkEnumeratePhysicalDevices)                      \
+  X(vkGetPhysicalDeviceMemoryProperties) X(vkCreateDevice) X(vkDestroyDevice)                 \
+  X(vkGetDeviceQueue) X(vkQueueSubmit) X(vkQueueWaitIdle) X(vkAllocateMemory) X(vkFreeMemory) \
+  X(vkMapMemory) X(vkUnmapMemory) X(vkBindBufferMemory) X(vkBindImageMemory)                  \
+  X(vkGetBufferMemoryRequirements) X(vkGetImageMemoryRequirements) X(vkCreateFence)           \
+  X(vkDestroyFence) X(vkResetFences) X(vkWaitForFences) X(vkCreateBuffer) X(vkDestroyBuffer)  \
+  X(vkCreateImage) X(vkDestroyImage) X(vkCreateImageView) X(vkDestroyImageView)               \
+  X(vkCreateShaderModule) X(vkDestroyShaderModule) X(vkCreateGraphicsPipelines)               \
+  X(vkDestroyPipeline) X(vkCreatePipelineLayout) X(vkDestroyPipelineLayout)                   \
+  X(vkCreateSampler) X(vkDestroySampler) X(vkCreateDescriptorSetLayout)                       \
+  X(vkDestroyDescriptorSetLayout) X(vkCreateDescriptorPool) X(vkDestroyDescriptorPool)        \
+  X(vkAllocateDescriptorSets) X(vkFreeDescriptorSets) X(vkUpdateDescriptorSets)               \
+  X(vkCreateFramebuffer) X(vkDestroyFramebuffer) X(vkCreateRenderPass)                        \
+  X(vkDestroyRenderPass) X(vkCreateCommandPool) X(vkDestroyCommandPool)                       \
+  X(vkAllocateCommandBuffers) X(vkFreeCommandBuffers) X(vkBeginCommandBuffer)                 \
+  X(vkEndCommandBuffer) X(vkCmdBindPipeline) X(vkCmdBindDescriptorSets)                       \
+  X(vkCmdBindIndexBuffer) X(vkCmdBindVertexBuffers) X(vkCmdDraw) X(vkCmdDrawIndexed)          \
+  X(vkCmdCopyBuffer) X(vkCmdCopyBufferToImage) X(vkCmdPushConstants)                          \
+  X(vkCmdBeginRenderPass) X(vkCmdEndRenderPass)
+  VSD_FNS(VSD_FN)
+#undef VSD_FN
+};
+}    // namespace
+
+struct vsd_context
+{
+  Fns fn;
+  vsd_get_proc_fn gpa = nullptr;
+  VkInstance instance = VK_NULL_HANDLE;
+  bool own_instance = false;
+  VkPhysicalDevice phys = VK_NULL_HANDLE;
+  VkDevice device = VK_NULL_HANDLE;
+  VkQueue queue = VK_NULL_HANDLE;
+  uint32_t type_device = 0, type_host = 1;
+};
+
+namespace
+{
+struct Alloc
+{
+  VkDeviceMemory mem = VK_NULL_HANDLE;
+  VkDeviceSize size = 0;
+};
+
+struct TargetObjs
+{
+  VkImage color = VK_NULL_HANDLE, depth = VK_NULL_HANDLE;
+  VkImageView color_view = VK_NULL_HANDLE, depth_view = VK_NULL_HANDLE;
+  Alloc color_mem, depth_mem;
+  VkFramebuffer fb = VK_NULL_HANDLE;
+  uint32_t width = 0, height = 0;
+};
+
+struct TextureObjs
+{
+  VkImage image = VK_NULL_HANDLE;
+  VkImageView view = VK_NULL_HANDLE;
+  Alloc mem;
+  VkBuffer staging = VK_NULL_HANDLE;
+  Alloc staging_mem;
+};
+}    // namespace
+
+struct vsd_scene
+{
+  vsd_context *ctx = nullptr;
+  const vsc_scene *scene = nullptr;
+  uint32_t flags = 0;
+  VkBuffer vb = VK_NULL_HANDLE, ib = VK_NULL_HANDLE, vb_stage = VK_NULL_HANDLE,
+           ib_stage = VK_NULL_HANDLE;
+  Alloc vb_mem, ib_mem, vb_stage_mem, ib_stage_mem;
+  std::vector<TextureObjs> textures;
+  std::vector<TargetObjs> targets;
+  VkSampler samplers[3] = {VK_NULL_HANDLE, VK_NULL_HANDLE, VK_NULL_HANDLE};
+  VkDescriptorSetLayout dsl = VK_NULL_HANDLE;
+  VkPipelineLayout layout = VK_NULL_HANDLE;
+  VkDescriptorPool pool = VK_NULL_HANDLE;
+  std::vector<VkDescriptorSet> sets; /* [texture * 3 + filter] */
+  std::vector<VkShaderModule> modules;
+  std::vector<VkPipeline> pipelines;
+  VkRenderPass rp_clear = VK_NULL_HANDLE, rp_load = VK_NULL_HANDLE;
+  VkCommandPool cmd_pool = VK_NULL_HANDLE;
+  VkCommandBuffer cmd = VK_NULL_HANDLE;
+  VkFence fence = VK_NULL_HANDLE;
+  uint64_t restage_bytes = 0;
+};
+
+#define VSD_CHECK(expr)          \
+  do                             \
+  {                              \
+    VkResult r_ = (expr);        \
+    if(r_ != VK_SUCCESS)         \
+      return (int)r_;            \
+  } while(0)
+
+extern "C" int vsd_create(vsd_get_proc_fn gpa, void *instance, vsd_context **out)
+{
+  vsd_context *c = new vsd_context();
+  c->gpa = gpa;
+  Fns &f = c->fn;
+  f.vkCreateInstance = (PFN_vkCreateInstance)gpa(nullptr, "vkCreateInstance");
+  if(instance)
+  {
+    c->instance = (VkInstance)instance;
+  }
+  else
+  {
+    VkApplicationInfo app = {};
+    app.sType = VK_STRUCTURE_TYPE_APPLICATION_INFO;
+    app.pApplicationName = "visor-scene";
+    app.apiVersion = VK_MAKE_VERSION(1, 0, 0);
+    VkInstanceCreateInfo ici = {};
+    ici.sType = VK_STRUCTURE_TYPE_INSTANCE_CREATE_INFO;
+    ici.pApplicationInfo = &app;
+    VkResult r = f.vkCreateInstance(&ici, nullptr, &c->instance);
+    if(r != VK_SUCCESS)
+    {
+      delete c;
+      return (int)r;
+    }
+    c->own_instance = true;
+  }
+#define VSD_LOAD(name) f.name = (PFN_##name)gpa((void *)c->instance, #name);
+  VSD_FNS(VSD_LOAD)
+#undef VSD_LOAD
+
+  uint32_t n = 1;
+  VSD_CHECK(f.vkEnumeratePhysicalDevices(c->instance, &n, nullptr));
+  n = 1;
+  VSD_CHECK(f.vkEnumeratePhysicalDevices(c->instance, &n, &c->phys));
+
+  VkPhysicalDeviceMemoryProperties mp;
+  memset(&mp, 0, sizeof(mp));
+  f.vkGetPhysicalDeviceMemoryProperties(c->phys, &mp);
+  for(uint32_t i = 0; i < mp.memoryTypeCount; i++)
+  {
+    VkMemoryPropertyFlags fl = mp.memoryTypes[i].propertyFlags;
+    if((fl & VK_MEMORY_PROPERTY_DEVICE_LOCAL_BIT) && !(fl & VK_MEMORY_PROPERTY_HOST_VISIBLE_BIT))
+      c->type_device = i;
+    if(fl & VK_MEMORY_PROPERTY_HOST_VISIBLE_BIT)
+      c->type_host = i;
+  }
+
+  float prio = 1.0f;
+  VkDeviceQueueCreateInfo qci = {};
+  qci.sType = VK_STRUCTURE_TYPE_DEVICE_QUEUE_CREATE_INFO;
+  qci.queueFamilyIndex = 0;
+  qci.queueCount = 1;
+  qci.pQueuePriorities = &prio;
+  VkDeviceCreateInfo dci = {};
+  dci.sType = VK_STRUCTURE_TYPE_DEVICE_CREATE_INFO;
+  dci.queueCreateInfoCount = 1;
+  dci.pQueueCreateInfos = &qci;
+  VSD_CHECK(f.vkCreateDevice(c->phys, &dci, nullptr, &c->device));
+  f.vkGetDeviceQueue(c->device, 0, 0, &c->queue);
+  *out = c;
+  return 0;
+}
+
+extern "C" void vsd_destroy(vsd_context *c)
+{
+  if(!c)
+    return;
+  if(c->device)
+    c->fn.vkDestroyDevice(c->device, nullptr);
+  if(c->own_instance && c->instance)
+    c->fn.vkDestroyInstance(c->instance, nullptr);
+  delete c;
+}
+
+static int make_buffer(vsd_context *c, VkDeviceSize size, VkBufferUsageFlags usage, uint32_t type,
+                       VkBuffer *buf, Alloc *a)
+{
+  Fns &f = c->fn;
+  VkBufferCreateInfo bci = {};
+  bci.sType = VK_STRUCTURE_TYPE_BUFFER_CREATE_INFO;
+  bci.size = size ? size : 4;
+  bci.usage = usage;
+  VSD_CHECK(f.vkCreateBuffer(c->device, &bci, nullptr, buf));
+  VkMemoryRequirements req;
+  f.vkGetBufferMemoryRequirements(c->device, *buf, &req);
+  VkMemoryAllocateInfo mai = {};
+  mai.sType = VK_STRUCTURE_TYPE_MEMORY_ALLOCATE_INFO;
+  mai.allocationSize = req.size;
+  mai.memoryTypeIndex = type;
+  VSD_CHECK(f.vkAllocateMemory(c->device, &mai, nullptr, &a->mem));
+  a->size = req.size;
+  VSD_CHECK(f.vkBindBufferMemory(c->device, *buf, a->mem, 0));
+  return 0;
+}
+
+static int fill_memory(vsd_context *c, Alloc *a, const void *src, VkDeviceSize bytes)
+{
+  void *dst = nullptr;
+  VSD_CHECK(c->fn.vkMapMemory(c->device, a->mem, 0, bytes, 0, &dst));
+  memcpy(dst, src, (size_t)bytes);
+  c->fn.vkUnmapMemory(c->device, a->mem);
+  return 0;
+}
+
+static int make_image(vsd_context *c, uint32_t w, uint32_t h, uint32_t mips, VkFormat fmt,
+                      VkImageUsageFlags usage, uint32_t type, VkImageAspectFlags aspect,
+                      VkImage *img, Alloc *a, VkImageView *view)
+{
+  Fns &f = c->fn;
+  VkImageCreateInfo ici = {};
+  ici.sType = VK_STRUCTURE_TYPE_IMAGE_CREATE_INFO;
+  ici.imageType = VK_IMAGE_TYPE_2D;
+  ici.format = fmt;
+  ici.extent.width = w;
+  ici.extent.height = h;
+  ici.extent.depth = 1;
+  ici.mipLevels = mips;
+  ici.arrayLayers = 1;
+  ici.samples = VK_SAMPLE_COUNT_1_BIT;
+  ici.tiling = type == c->type_host ? VK_IMAGE_TILING_LINEAR : VK_IMAGE_TILING_OPTIMAL;
+  ici.usage = usage;
+  ici.initialLayout = VK_IMAGE_LAYOUT_UNDEFINED;
+  VSD_CHECK(f.vkCreateImage(c->device, &ici, nullptr, img));
+  VkMemoryRequirements req;
+  f.vkGetImageMemoryRequirements(c->device, *img, &req);
+  VkMemoryAllocateInfo mai = {};
+  mai.sType = VK_STRUCTURE_TYPE_MEMORY_ALLOCATE_INFO;
+  mai.allocationSize = req.size;
+  mai.memoryTypeIndex = type;
+  VSD_CHECK(f.vkAllocateMemory(c->device, &mai, nullptr, &a->mem));
+  a->size = req.size;
+  VSD_CHECK(f.vkBindImageMemory(c->device, *img, a->mem, 0));
+  VkImageViewCreateInfo vci = {};
+  vci.sType = VK_STRUCTURE_TYPE_IMAGE_VIEW_CREATE_INFO;
+  vci.image = *img;
+  vci.viewType = VK_IMAGE_VIEW_TYPE_2D;
+  vci.format = fmt;
+  vci.subresourceRange.aspectMask = aspect;
+  vci.subresourceRange.levelCount = mips;
+  vci.subresourceRange.layerCount = 1;
+  VSD_CHECK(f.vkCreateImageView(c->device, &vci, nullptr, view));
+  return 0;
+}
+
+static int make_render_pass(vsd_context *c, bool clear, VkRenderPass *rp)
+{
+  VkAttachmentDescription att[2];
+  memset(att, 0, sizeof(att));
+  att[0].format = VK_FORMAT_R8G8B8A8_UNORM;
+  att[0].samples = VK_SAMPLE_COUNT_1_BIT;
+  att[0].loadOp = clear ? VK_ATTACHMENT_LOAD_OP_CLEAR : VK_ATTACHMENT_LOAD_OP_LOAD;
+  att[0].storeOp = VK_ATTACHMENT_STORE_OP_STORE;
+  att[0].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_DONT_CARE;
+  att[0].stencilStoreOp = VK_ATTACHMENT_STORE_OP_DONT_CARE;
+  att[0].initialLayout = VK_IMAGE_LAYOUT_UNDEFINED;
+  att[0].finalLayout = VK_IMAGE_LAYOUT_GENERAL;
+  att[1] = att[0];
+  att[1].format = VK_FORMAT_D32_SFLOAT;
+  VkAttachmentReference cref = {0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL};
+  VkAttachmentReference dref = {1, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
+  VkSubpassDescription sub = {};
+  sub.pipelineBindPoint = VK_PIPELINE_BIND_POINT_GRAPHICS;
+  sub.colorAttachmentCount = 1;
+  sub.pColorAttachments = &cref;
+  sub.pDepthStencilAttachment = &dref;
+  VkRenderPassCreateInfo rci = {};
+  rci.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
+  rci.attachmentCount = 2;
+  rci.pAttachments = att;
+  rci.subpassCount = 1;
+  rci.pSubpasses = &sub;
+  VSD_CHECK(c->fn.vkCreateRenderPass(c->device, &rci, nullptr, rp));
+  return 0;
+}
+
+static int make_pipeline(vsd_scene *s, const vsc_pipeline &p, VkPipeline *out)
+{
+  vsd_context *c = s->ctx;
+  Fns &f = c->fn;
+  VkShaderModule mods[2];
+  for(int st = 0; st < 2; st++)
+  {
+    uint32_t stage = st == 0 ? VSPV_STAGE_VERTEX : VSPV_STAGE_FRAGMENT;
+    size_t n = vspv_emit(p.shader, stage, nullptr, 0);
+    if(!n)
+      return (int)VK_ERROR_INITIALIZATION_FAILED;
+    std::vector<uint32_t> words(n);
+    vspv_emit(p.shader, stage, words.data(), n);
+    VkShaderModuleCreateInfo smci = {};
+    smci.sType = VK_STRUCTURE_TYPE_SHADER_MODULE_CREATE_INFO;
+    smci.codeSize = n * 4;
+    smci.pCode = words.data();
+    VSD_CHECK(f.vkCreateShaderModule(c->device, &smci, nullptr, &mods[st]));
+    s->modules.push_back(mods[st]);
+  }
+  VkPipelineShaderStageCreateInfo stages[2] = {};
+  for(int st = 0; st < 2; st++)
+  {
+    stages[st].sType = VK_STRUCTURE_TYPE_PIPELINE_SHADER_STAGE_CREATE_INFO;
+    stages[st].stage = st == 0 ? VK_SHADER_STAGE_VERTEX_BIT : VK_SHADER_STAGE_FRAGMENT_BIT;
+    stages[st].module = mods[st];
+    stages[st].pName = "main";
+  }
+  vsc_attr attrs[4];
+  uint32_t na = vsc_vertex_attrs(p.shader, attrs);
+  VkVertexInputBindingDescription bind = {0, vsc_stride_of(p.shader), VK_VERTEX_INPUT_RATE_VERTEX};
+  VkVertexInputAttributeDescription vad[4];
+  for(uint32_t i = 0; i < na; i++)
+  {
+    vad[i].location = attrs[i].location;
+    vad[i].binding = 0;
+    vad[i].format = (VkFormat)attrs[i].format;
+    vad[i].offset = attrs[i].offset;
+  }
+  VkPipelineVertexInputStateCreateInfo vi = {};
+  vi.sType = VK_STRUCTURE_TYPE_PIPELINE_VERTEX_INPUT_STATE_CREATE_INFO;
+  vi.vertexBindingDescriptionCount = 1;
+  vi.pVertexBindingDescriptions = &bind;
+  vi.vertexAttributeDescriptionCount = na;
+  vi.pVertexAttributeDescriptions = vad;
+  VkPipelineInputAssemblyStateCreateInfo ia = {};
+  ia.sType = VK_STRUCTURE_TYPE_PIPELINE_INPUT_ASSEMBLY_STATE_CREATE_INFO;
+  ia.topology = (VkPrimitiveTopology)p.topology;
+  uint32_t w = s->scene->num_targets ? s->scene->targets[0].width : 1;
+  uint32_t h = s->scene->num_targets ? s->scene->targets[0].height : 1;
+  VkViewport vp = {0.0f, 0.0f, (float)w, (float)h, 0.0f, 1.0f};
+  VkRect2D sc = {{0, 0}, {w, h}};
+  VkPipelineViewportStateCreateInfo vps = {};
+  vps.sType = VK_STRUCTURE_TYPE_PIPELINE_VIEWPORT_STATE_CREATE_INFO;
+  vps.viewportCount = 1;
+  vps.pViewports = &vp;
+  vps.scissorCount = 1;
+  vps.pScissors = &sc;
+  VkPipelineRasterizationStateCreateInfo rs = {};
+  rs.sType = VK_STRUCTURE_TYPE_PIPELINE_RASTERIZATION_STATE_CREATE_INFO;
+  rs.polygonMode = VK_POLYGON_MODE_FILL;
+  rs.cullMode = p.cull_mode;
+  rs.frontFace = (VkFrontFace)p.front_face;
+  rs.lineWidth = 1.0f;
+  VkPipelineMultisampleStateCreateInfo ms = {};
+  ms.sType = VK_STRUCTURE_TYPE_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO;
+  ms.rasterizationSamples = VK_SAMPLE_COUNT_1_BIT;
+  VkPipelineDepthStencilStateCreateInfo ds = {};
+  ds.sType = VK_STRUCTURE_TYPE_PIPELINE_DEPTH_STENCIL_STATE_CREATE_INFO;
+  ds.depthTestEnable = VK_TRUE;
+  ds.depthWriteEnable = p.depth_write ? VK_TRUE : VK_FALSE;
+  ds.depthCompareOp = (VkCompareOp)p.depth_op;
+  VkPipelineColorBlendAttachmentState cba = {};
+  cba.blendEnable = p.blend_enable ? VK_TRUE : VK_FALSE;
+  cba.srcColorBlendFactor = (VkBlendFactor)p.src_factor;
+  cba.dstColorBlendFactor = (VkBlendFactor)p.dst_factor;
+  cba.colorBlendOp = VK_BLEND_OP_ADD;
+  cba.srcAlphaBlendFactor = (VkBlendFactor)p.src_factor;
+  cba.dstAlphaBlendFactor = (VkBlendFactor)p.dst_factor;
+  cba.alphaBlendOp = VK_BLEND_OP_ADD;
+  cba.colorWriteMask = 0xf;
+  VkPipelineColorBlendStateCreateInfo cb = {};
+  cb.sType = VK_STRUCTURE_TYPE_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO;
+  cb.attachmentCount = 1;
+  cb.pAttachments = &cba;
+  VkGraphicsPipelineCreateInfo gci = {};
+  gci.sType = VK_STRUCTURE_TYPE_GRAPHICS_PIPELINE_CREATE_INFO;
+  gci.stageCount = 2;
+  gci.pStages = stages;
+  gci.pVertexInputState = &vi;
+  gci.pInputAssemblyState = &ia;
+  gci.pViewportState = &vps;
+  gci.pRasterizationState = &rs;
+  gci.pMultisampleState = &ms;
+  gci.pDepthStencilState = p.depth_test ? &ds : nullptr;
+  gci.pColorBlendState = &cb;
+  gci.layout = s->layout;
+  gci.renderPass = s->rp_clear;
+  VSD_CHECK(f.vkCreateGraphicsPipelines(c->device, VK_NULL_HANDLE, 1, &gci, nullptr, out));
+  return 0;
+}
+
+static int record(vsd_scene *s)
+{
+  vsd_context *c = s->ctx;
+  Fns &f = c->fn;
+  const vsc_scene *sc = s->scene;
+  VkCommandBufferBeginInfo bi = {};
+  bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+  VSD_CHECK(f.vkBeginCommandBuffer(s->cmd, &bi));
+  if(s->flags & VSD_RESTAGE_INPUTS)
+  {
+    if(sc->vb_bytes)
+    {
+      VkBufferCopy r = {0, 0, sc->vb_bytes};
+      f.vkCmdCopyBuffer(s->cmd, s->vb_stage, s->vb, 1, &r);
+    }
+    if(sc->ib_count)
+    {
+      VkBufferCopy r = {0, 0, sc->ib_count * 4};
+      f.vkCmdCopyBuffer(s->cmd, s->ib_stage, s->ib, 1, &r);
+    }
+  }
+  for(uint32_t pi = 0; pi < sc->num_passes; pi++)
+  {
+    const vsc_pass &pass = sc->passes[pi];
+    TargetObjs &t = s->targets[pass.target];
+    VkClearValue cv[2];
+    memset(cv, 0, sizeof(cv));
+    for(int i = 0; i < 4; i++)
+      cv[0].color.float32[i] = sc->clear_color[i];
+    cv[1].depthStencil.depth = sc->clear_depth;
+    VkRenderPassBeginInfo rbi = {};
+    rbi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_BEGIN_INFO;
+    rbi.renderPass = pass.clear ? s->rp_clear : s->rp_load;
+    rbi.framebuffer = t.fb;
+    rbi.renderArea.extent.width = t.width;
+    rbi.renderArea.extent.height = t.height;
+    rbi.clearValueCount = 2;
+    rbi.pClearValues = cv;
+    f.vkCmdBeginRenderPass(s->cmd, &rbi, VK_SUBPASS_CONTENTS_INLINE);
+    if(sc->ib_count)
+      f.vkCmdBindIndexBuffer(s->cmd, s->ib, 0, VK_INDEX_TYPE_UINT32);
+    uint32_t cur_pipe = ~0u, cur_set = ~0u;
+    for(uint32_t di = pass.first_draw; di < pass.first_draw + pass.draw_count; di++)
+    {
+      const vsc_draw &d = sc->draws[di];
+      const vsc_pipeline &p = sc->pipelines[d.pipeline];
+      if(d.pipeline != cur_pipe)
+      {
+        f.vkCmdBindPipeline(s->cmd, VK_PIPELINE_BIND_POINT_GRAPHICS, s->pipelines[d.pipeline]);
+        cur_pipe = d.pipeline;
+      }
+      if(d.texture != VSC_NONE)
+      {
+        uint32_t set = d.texture * 3 + p.filter;
+        if(set != cur_set)
+        {
+          f.vkCmdBindDescriptorSets(s->cmd, VK_PIPELINE_BIND_POINT_GRAPHICS, s->layout, 0, 1,
+                                    &s->sets[set], 0, nullptr);
+          cur_set = set;
+        }
+      }
+      VkDeviceSize off = d.vb_offset;
+      f.vkCmdBindVertexBuffers(s->cmd, 0, 1, &s->vb, &off);
+      if(d.push_size)
+        f.vkCmdPushConstants(s->cmd, s->layout,
+                             VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0,
+                             d.push_size, d.push);
+      if(d.indexed)
+        f.vkCmdDrawIndexed(s->cmd, d.count, 1, d.first, 0, 0);
+      else
+        f.vkCmdDraw(s->cmd, d.count, 1, d.first, 0);
+    }
+    f.vkCmdEndRenderPass(s->cmd);
+  }
+  VSD_CHECK(f.vkEndCommandBuffer(s->cmd));
+  return 0;
+}
+
+static int submit_one(vsd_scene *s, VkCommandBuffer cmd)
+{
+  Fns &f = s->ctx->fn;
+  VkSubmitInfo si = {};
+  si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+  si.commandBufferCount = 1;
+  si.pCommandBuffers = &cmd;
+  VSD_CHECK(f.vkQueueSubmit(s->ctx->queue, 1, &si, s->fence));
+  VSD_CHECK(f.vkWaitForFences(s->ctx->device, 1, &s->fence, VK_TRUE, ~0ull));
+  VSD_CHECK(f.vkResetFences(s->ctx->device, 1, &s->fence));
+  return 0;
+}
+
+extern "C" int vsd_upload(vsd_context *c, const vsc_scene *sc, uint32_t flags, vsd_scene **out)
+{
+  Fns &f = c->fn;
+  vsd_scene *s = new vsd_scene();
+  *out = s;
+  s->ctx = c;
+  s->scene = sc;
+  s->flags = flags;
+  int rc;
+#define TRY(x)        \
+  do                  \
+  {                   \
+    rc = (x);         \
+    if(rc)            \
+      return rc;      \
+  } while(0)
+
+  VkFenceCreateInfo fci = {};
+  fci.sType = VK_STRUCTURE_TYPE_FENCE_CREATE_INFO;
+  VSD_CHECK(f.vkCreateFence(c->device, &fci, nullptr, &s->fence));
+  VkCommandPoolCreateInfo cpci = {};
+  cpci.sType = VK_STRUCTURE_TYPE_COMMAND_POOL_CREATE_INFO;
+  VSD_CHECK(f.vkCreateCommandPool(c->device, &cpci, nullptr, &s->cmd_pool));
+  VkCommandBufferAllocateInfo cbai = {};
+  cbai.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_ALLOCATE_INFO;
+  cbai.commandPool = s->cmd_pool;
+  cbai.level = VK_COMMAND_BUFFER_LEVEL_PRIMARY;
+  cbai.commandBufferCount = 1;
+  VkCommandBuffer upload = VK_NULL_HANDLE;
+  VSD_CHECK(f.vkAllocateCommandBuffers(c->device, &cbai, &upload));
+  VSD_CHECK(f.vkAllocateCommandBuffers(c->device, &cbai, &s->cmd));
+
+  /* geometry: host-visible staging copied into device-local buffers */
+  TRY(make_buffer(c, sc->vb_bytes, VK_BUFFER_USAGE_TRANSFER_SRC_BIT, c->type_host, &s->vb_stage,
+                  &s->vb_stage_mem));
+  TRY(make_buffer(c, sc->vb_bytes, VK_BUFFER_USAGE_VERTEX_BUFFER_BIT | VK_BUFFER_USAGE_TRANSFER_DST_BIT,
+                  c->type_device, &s->vb, &s->vb_mem));
+  TRY(make_buffer(c, sc->ib_count * 4, VK_BUFFER_USAGE_TRANSFER_SRC_BIT, c->type_host,
+                  &s->ib_stage, &s->ib_stage_mem));
+  TRY(make_buffer(c, sc->ib_count * 4,
+                  VK_BUFFER_USAGE_INDEX_BUFFER_BIT | VK_BUFFER_USAGE_TRANSFER_DST_BIT,
+                  c->type_device, &s->ib, &s->ib_mem));
+  if(sc->vb_bytes)
+    TRY(fill_memory(c, &s->vb_stage_mem, sc->vb, sc->vb_bytes));
+  if(sc->ib_count)
+    TRY(fill_memory(c, &s->ib_stage_mem, sc->ib, sc->ib_count * 4));
+  s->restage_bytes = sc->vb_bytes + sc->ib_count * 4;
+
+  /* textures: staging buffer with every mip, copied per mip */
+  s->textures.resize(sc->num_textures);
+  for(uint32_t t = 0; t < sc->num_textures; t++)
+  {
+    const vsc_texture &tx = sc->textures[t];
+    TextureObjs &o = s->textures[t];
+    TRY(make_image(c, tx.width, tx.height, tx.mips, VK_FORMAT_R8G8B8A8_UNORM,
+                   VK_IMAGE_USAGE_SAMPLED_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT, c->type_device,
+                   VK_IMAGE_ASPECT_COLOR_BIT, &o.image, &o.mem, &o.view));
+    TRY(make_buffer(c, tx.bytes, VK_BUFFER_USAGE_TRANSFER_SRC_BIT, c->type_host, &o.staging,
+                    &o.staging_mem));
+    TRY(fill_memory(c, &o.staging_mem, tx.texels, tx.bytes));
+  }
+
+  /* render targets: colour + depth, host-visible so results can be mapped */
+  uint32_t ttype = (flags & VSD_DEVICE_TARGETS) ? c->type_device : c->type_host;
+  TRY(make_render_pass(c, true, &s->rp_clear));
+  TRY(make_render_pass(c, false, &s->rp_load));
+  s->targets.resize(sc->num_targets);
+  for(uint32_t t = 0; t < sc->num_targets; t++)
+  {
+    TargetObjs &o = s->targets[t];
+    o.width = sc->targets[t].width;
+    o.height = sc->targets[t].height;
+    TRY(make_image(c, o.width, o.height, 1, VK_FORMAT_R8G8B8A8_UNORM,
+                   VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT, ttype, VK_IMAGE_ASPECT_COLOR_BIT, &o.color,
+                   &o.color_mem, &o.color_view));
+    TRY(make_image(c, o.width, o.height, 1, VK_FORMAT_D32_SFLOAT,
+                   VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT, ttype, VK_IMAGE_ASPECT_DEPTH_BIT,
+                   &o.depth, &o.depth_mem, &o.depth_view));
+    VkImageView views[2] = {o.color_view, o.depth_view};
+    VkFramebufferCreateInfo fbci = {};
+    fbci.sType = VK_STRUCTURE_TYPE_FRAMEBUFFER_CREATE_INFO;
+    fbci.renderPass = s->rp_clear;
+    fbci.attachmentCount = 2;
+    fbci.pAttachments = views;
+    fbci.width = o.width;
+    fbci.height = o.height;
+    fbci.layers = 1;
+    VSD_CHECK(f.vkCreateFramebuffer(c->device, &fbci, nullptr, &o.fb));
+  }
+
+  /* samplers: the reference's bilinear mip 0, trilinear over the chain, nearest */
+  for(int k = 0; k < 3; k++)
+  {
+    VkSamplerCreateInfo sci = {};
+    sci.sType = VK_STRUCTURE_TYPE_SAMPLER_CREATE_INFO;
+    sci.magFilter = k == VSC_FILTER_NEAREST ? VK_FILTER_NEAREST : VK_FILTER_LINEAR;
+    sci.minFilter = sci.magFilter;
+    sci.mipmapMode = k == VSC_FILTER_TRILINEAR ? VK_SAMPLER_MIPMAP_MODE_LINEAR
+                                               : VK_SAMPLER_MIPMAP_MODE_NEAREST;
+    sci.addressModeU = sci.addressModeV = sci.addressModeW = VK_SAMPLER_ADDRESS_MODE_REPEAT;
+    sci.maxLod = k == VSC_FILTER_TRILINEAR ? 1000.0f : 0.0f;
+    VSD_CHECK(f.vkCreateSampler(c->device, &sci, nullptr, &s->samplers[k]));
+  }
+  VkDescriptorSetLayoutBinding b = {};
+  b.binding = 0;
+  b.descriptorType = VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER;
+  b.descriptorCount = 1;
+  b.stageFlags = VK_SHADER_STAGE_FRAGMENT_BIT;
+  VkDescriptorSetLayoutCreateInfo dslci = {};
+  dslci.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO;
+  dslci.bindingCount = 1;
+  dslci.pBindings = &b;
+  VSD_CHECK(f.vkCreateDescriptorSetLayout(c->device, &dslci, nullptr, &s->dsl));
+  VkPushConstantRange pcr = {VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0, 128};
+  VkPipelineLayoutCreateInfo plci = {};
+  plci.sType = VK_STRUCTURE_TYPE_PIPELINE_LAYOUT_CREATE_INFO;
+  plci.setLayoutCount = 1;
+  plci.pSetLayouts = &s->dsl;
+  plci.pushConstantRangeCount = 1;
+  plci.pPushConstantRanges = &pcr;
+  VSD_CHECK(f.vkCreatePipelineLayout(c->device, &plci, nullptr, &s->layout));
+  VkDescriptorPoolSize ps = {VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER,
+                             sc->num_textures * 3 + 1};
+  VkDescriptorPoolCreateInfo dpci = {};
+  dpci.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_POOL_CREATE_INFO;
+  dpci.maxSets = sc->num_textures * 3 + 1;
+  dpci.poolSizeCount = 1;
+  dpci.pPoolSizes = &ps;
+  VSD_CHECK(f.vkCreateDescriptorPool(c->device, &dpci, nullptr, &s->pool));
+  s->sets.assign((size_t)sc->num_textures * 3, VK_NULL_HANDLE);
+  for(uint32_t t = 0; t < sc->num_textures; t++)
+  {
+    for(int k = 0; k < 3; k++)
+    {
+      /* one set per call: the reference writes only pDescriptorSets[0] (descriptors.cpp:54-65) */
+      VkDescriptorSetAllocateInfo dsai = {};
+      dsai.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_ALLOCATE_INFO;
+      dsai.descriptorPool = s->pool;
+      dsai.descriptorSetCount = 1;
+      dsai.pSetLayouts = &s->dsl;
+      VkDescriptorSet set = VK_NULL_HANDLE;
+      VSD_CHECK(f.vkAllocateDescriptorSets(c->device, &dsai, &set));
+      VkDescriptorImageInfo ii = {s->samplers[k], s->textures[t].view,
+                                  VK_IMAGE_LAYOUT_SHADER_READ_ONLY_OPTIMAL};
+      VkWriteDescriptorSet w = {};
+      w.sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;
+      w.dstSet = set;
+      w.dstBinding = 0;
+      w.descriptorCount = 1;
+      w.descriptorType = VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER;
+      w.pImageInfo = &ii;
+      f.vkUpdateDescriptorSets(c->device, 1, &w, 0, nullptr);
+      s->sets[t * 3 + k] = set;
+    }
+  }
+
+  s->pipelines.resize(sc->num_pipelines);
+  for(uint32_t p = 0; p < sc->num_pipelines; p++)
+    TRY(make_pipeline(s, sc->pipelines[p], &s->pipelines[p]));
+
+  /* one-time upload */
+  VkCommandBufferBeginInfo bi = {};
+  bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+  VSD_CHECK(f.vkBeginCommandBuffer(upload, &bi));
+  if(sc->vb_bytes)
+  {
+    VkBufferCopy r = {0, 0, sc->vb_bytes};
+    f.vkCmdCopyBuffer(upload, s->vb_stage, s->vb, 1, &r);
+  }
+  if(sc->ib_count)
+  {
+    VkBufferCopy r = {0, 0, sc->ib_count * 4};
+    f.vkCmdCopyBuffer(upload, s->ib_stage, s->ib, 1, &r);
+  }
+  for(uint32_t t = 0; t < sc->num_textures; t++)
+  {
+    const vsc_texture &tx = sc->textures[t];
+    for(uint32_t m = 0; m < tx.mips; m++)
+    {
+      VkBufferImageCopy r = {};
+      r.bufferOffset = vsc_texture_mip_offset(&tx, m);
+      r.imageSubresource.aspectMask = VK_IMAGE_ASPECT_COLOR_BIT;
+      r.imageSubresource.mipLevel = m;
+      r.imageSubresource.layerCount = 1;
+      r.imageExtent.width = (tx.width >> m) ? (tx.width >> m) : 1;
+      r.imageExtent.height = (tx.height >> m) ? (tx.height >> m) : 1;
+      r.imageExtent.depth = 1;
+      f.vkCmdCopyBufferToImage(upload, s->textures[t].staging, s->textures[t].image,
+                               VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &r);
+    }
+  }
+  VSD_CHECK(f.vkEndCommandBuffer(upload));
+  TRY(submit_one(s, upload));
+  f.vkFreeCommandBuffers(c->device, s->cmd_pool, 1, &upload);
+
+  TRY(record(s));
+#undef TRY
+  return 0;
+}
+
+extern "C" int vsd_submit(vsd_scene *s) { return submit_one(s, s->cmd); }
+
+extern "C" int vsd_submit_async(vsd_scene *s)
+{
+  Fns &f = s->ctx->fn;
+  VkSubmitInfo si = {};
+  si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+  si.commandBufferCount = 1;
+  si.pCommandBuffers = &s->cmd;
+  VSD_CHECK(f.vkQueueSubmit(s->ctx->queue, 1, &si, s->fence));
+  return 0;
+}
+
+extern "C" int vsd_wait(vsd_scene *s, uint64_t timeout_ns)
+{
+  Fns &f = s->ctx->fn;
+  VSD_CHECK(f.vkWaitForFences(s->ctx->device, 1, &s->fence, VK_TRUE, timeout_ns));
+  VSD_CHECK(f.vkResetFences(s->ctx->device, 1, &s->fence));
+  return 0;
+}
+
+extern "C" int vsd_read_target(vsd_scene *s, uint32_t target, uint8_t *color, float *depth)
+{
+  vsd_context *c = s->ctx;
+  TargetObjs &t = s->targets[target];
+  VkDeviceSize bytes = (VkDeviceSize)t.width * t.height * 4;
+  void *p = nullptr;
+  if(color)
+  {
+    VSD_CHECK(c->fn.vkMapMemory(c->device, t.color_mem.mem, 0, bytes, 0, &p));
+    memcpy(color, p, (size_t)bytes);
+    c->fn.vkUnmapMemory(c->device, t.color_mem.mem);
+  }
+  if(depth)
+  {
+    VSD_CHECK(c->fn.vkMapMemory(c->device, t.depth_mem.mem, 0, bytes, 0, &p));
+    memcpy(depth, p, (size_t)bytes);
+    c->fn.vkUnmapMemory(c->device, t.depth_mem.mem);
+  }
+  return 0;
+}
+
+extern "C" uint64_t vsd_restage_bytes(const vsd_scene *s) { return s->restage_bytes; }
+
+extern "C" void vsd_release(vsd_scene *s)
+{
+  if(!s)
+    return;
+  vsd_context *c = s->ctx;
+  Fns &f = c->fn;
+  VkDevice d = c->device;
+  for(VkPipeline p : s->pipelines)
+    if(p) f.vkDestroyPipeline(d, p, nullptr);
+  for(VkShaderModule m : s->modules)
+    if(m) f.vkDestroyShaderModule(d, m, nullptr);
+  for(TargetObjs &t : s->targets)
+  {
+    if(t.fb) f.vkDestroyFramebuffer(d, t.fb, nullptr);
+    if(t.color_view) f.vkDestroyImageView(d, t.color_view, nullptr);
+    if(t.depth_view) f.vkDestroyImageView(d, t.depth_view, nullptr);
+    if(t.color) f.vkDestroyImage(d, t.color, nullptr);
+    if(t.depth) f.vkDestroyImage(d, t.depth, nullptr);
+    if(t.color_mem.mem) f.vkFreeMemory(d, t.color_mem.mem, nullptr);
+    if(t.depth_mem.mem) f.vkFreeMemory(d, t.depth_mem.mem, nullptr);
+  }
+  for(TextureObjs &t : s->textures)
+  {
+    if(t.view) f.vkDestroyImageView(d, t.view, nullptr);
+    if(t.image) f.vkDestroyImage(d, t.image, nullptr);
+    if(t.mem.mem) f.vkFreeMemory(d, t.mem.mem, nullptr);
+    if(t.staging) f.vkDestroyBuffer(d, t.staging, nullptr);
+    if(t.staging_mem.mem) f.vkFreeMemory(d, t.staging_mem.mem, nullptr);
+  }
+  VkBuffer bufs[4] = {s->vb, s->ib, s->vb_stage, s->ib_stage};
+  Alloc *mems[4] = {&s->vb_mem, &s->ib_mem, &s->vb_stage_mem, &s->ib_stage_mem};
+  for(int i = 0; i < 4; i++)
+  {
+    if(bufs[i]) f.vkDestroyBuffer(d, bufs[i], nullptr);
+    if(mems[i]->mem) f.vkFreeMemory(d, mems[i]->mem, nullptr);
+  }
+  for(VkSampler smp : s->samplers)
+    if(smp) f.vkDestroySampler(d, smp, nullptr);
+  if(s->pool) f.vkDestroyDescriptorPool(d, s->pool, nullptr);
+  if(s->layout) f.vkDestroyPipelineLayout(d, s->layout, nullptr);
+  if(s->dsl) f.vkDestroyDescriptorSetLayout(d, s->dsl, nullptr);
+  if(s->rp_clear) f.vkDestroyRenderPass(d, s->rp_clear, nullptr);
+  if(s->rp_load) f.vkDestroyRenderPass(d, s->rp_load, nullptr);
+  if(s->cmd) f.vkFreeCommandBuffers(d, s->cmd_pool, 1, &s->cmd);
+  if(s->cmd_pool) f.vkDestroyCommandPool(d, s->cmd_pool, nullptr);
+  if(s->fence) f.vkDestroyFence(d, s->fence, nullptr);
+  delete s;
+}

@@ -1,0 +1,860 @@
+/*
+ * Seeded synthetic scenes for the Visor draw path (see include/visor_scene.h).
+ *
+ * Everything is generated on the host in double precision with the
+ * deterministic helpers below and rounded to float32, so every consumer (the
+ * CPU oracle, the reference build and the GPU driver) sees identical bytes on
+ * x86-64 and aarch64.  Compile with -ffp-contract=off.
+ */
+#include "visor_scene.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------ */
+/* deterministic math                                                        */
+/* ------------------------------------------------------------------------ */
+
+static const double kPi = 3.14159265358979323846;
+static const double kLn2 = 0.69314718055994530942;
+
+/* Round half away from zero without relying on the current rounding mode. */
+static double round_det(double x) { return x >= 0.0 ? floor(x + 0.5) : -floor(-x + 0.5); }
+
+/* sin/cos: reduce by multiples of pi/2, then Taylor series on [-pi/4, pi/4]. */
+static double sin_core(double r)
+{
+  double r2 = r * r, term = r, sum = r;
+  for(int k = 1; k <= 11; k++)
+  {
+    term = -term * r2 / (double)((2 * k) * (2 * k + 1));
+    sum = sum + term;
+  }
+  return sum;
+}
+
+static double cos_core(double r)
+{
+  double r2 = r * r, term = 1.0, sum = 1.0;
+  for(int k = 1; k <= 11; k++)
+  {
+    term = -term * r2 / (double)((2 * k - 1) * (2 * k));
+    sum = sum + term;
+  }
+  return sum;
+}
+
+double vsc_sin(double x)
+{
+  double k = round_det(x / (kPi * 0.5));
+  double r = x - k * (kPi * 0.5);
+  long q = ((long)k) & 3;
+  switch(q)
+  {
+    case 0: return sin_core(r);
+    case 1: return cos_core(r);
+    case 2: return -sin_core(r);
+    default: return -cos_core(r);
+  }
+}
+
+double vsc_cos(double x) { return vsc_sin(x + kPi * 0.5); }
+
+double vsc_exp(double x)
+{
+  double k = round_det(x / kLn2);
+  double r = x - k * kLn2;
+  double term = 1.0, sum = 1.0;
+  for(int i = 1; i <= 20; i++)
+  {
+    term = term * r / (double)i;
+    sum = sum + term;
+  }
+  return ldexp(sum, (int)k);
+}
+
+double vsc_log(double x)
+{
+  if(x <= 0.0)
+    return -1e300;
+  int e = 0;
+  double m = frexp(x, &e); /* x = m * 2^e, m in [0.5, 1) */
+  if(m < 0.70710678118654752440)
+  {
+    m = m * 2.0;
+    e = e - 1;
+  }
+  /* log(m) = 2 atanh((m-1)/(m+1)) */
+  double s = (m - 1.0) / (m + 1.0);
+  double s2 = s * s, term = s, sum = s;
+  for(int k = 1; k <= 30; k++)
+  {
+    term = term * s2;
+    sum = sum + term / (double)(2 * k + 1);
+  }
+  return 2.0 * sum + (double)e * kLn2;
+}
+
+/* ------------------------------------------------------------------------ */
+/* RNG: splitmix64, one stream per object                                    */
+/* ------------------------------------------------------------------------ */
+
+typedef struct rng { uint64_t s; } rng;
+
+static uint64_t splitmix(uint64_t *s)
+{
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static rng rng_for(uint64_t seed, uint32_t config, uint64_t object)
+{
+  rng r;
+  uint64_t s = seed ^ ((uint64_t)config << 56) ^ (object * 0xD1B54A32D192ED03ull);
+  r.s = splitmix(&s);
+  splitmix(&r.s);
+  return r;
+}
+
+static double urand(rng *r) { return (double)(splitmix(&r->s) >> 11) * (1.0 / 9007199254740992.0); }
+static uint32_t urand_u32(rng *r) { return (uint32_t)(splitmix(&r->s) >> 32); }
+static double loguniform(rng *r, double lo, double hi)
+{
+  return lo * vsc_exp(urand(r) * vsc_log(hi / lo));
+}
+
+uint64_t vsc_hash_bytes(const void *p, uint64_t n)
+{
+  const uint8_t *b = (const uint8_t *)p;
+  uint64_t h = 0xcbf29ce484222325ull;
+  for(uint64_t i = 0; i < n; i++)
+  {
+    h ^= b[i];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+/* ------------------------------------------------------------------------ */
+/* scene containers                                                          */
+/* ------------------------------------------------------------------------ */
+
+#define GROW(ptr, cap, need, type)                                    \
+  do                                                                  \
+  {                                                                   \
+    if((need) > (cap))                                                \
+    {                                                                 \
+      uint64_t ncap = (cap) ? (cap) : 4;                              \
+      while(ncap < (need))                                            \
+        ncap *= 2;                                                    \
+      ptr = (type *)realloc(ptr, (size_t)ncap * sizeof(type));        \
+      cap = ncap;                                                     \
+    }                                                                 \
+  } while(0)
+
+vsc_scene *vsc_new(void)
+{
+  vsc_scene *s = (vsc_scene *)calloc(1, sizeof(vsc_scene));
+  s->clear_color[0] = 0.0f;
+  s->clear_color[1] = 0.0f;
+  s->clear_color[2] = 0.0f;
+  s->clear_color[3] = 1.0f;
+  s->clear_depth = 1.0f;
+  return s;
+}
+
+void vsc_free(vsc_scene *s)
+{
+  if(!s)
+    return;
+  for(uint32_t i = 0; i < s->num_textures; i++)
+    free(s->textures[i].texels);
+  free(s->textures);
+  free(s->targets);
+  free(s->pipelines);
+  free(s->vb);
+  free(s->ib);
+  free(s->draws);
+  free(s->passes);
+  free(s);
+}
+
+uint32_t vsc_add_target(vsc_scene *s, uint32_t width, uint32_t height)
+{
+  uint64_t cap = s->cap_targets;
+  GROW(s->targets, cap, (uint64_t)s->num_targets + 1, vsc_target);
+  s->cap_targets = (uint32_t)cap;
+  s->targets[s->num_targets].width = width;
+  s->targets[s->num_targets].height = height;
+  return s->num_targets++;
+}
+
+uint32_t vsc_add_pipeline(vsc_scene *s, const vsc_pipeline *p)
+{
+  uint64_t cap = s->cap_pipelines;
+  GROW(s->pipelines, cap, (uint64_t)s->num_pipelines + 1, vsc_pipeline);
+  s->cap_pipelines = (uint32_t)cap;
+  s->pipelines[s->num_pipelines] = *p;
+  return s->num_pipelines++;
+}
+
+uint64_t vsc_texture_mip_offset(const vsc_texture *t, uint32_t mip)
+{
+  /* tight per-mip packing, as CalcSubresourceByteOffset (precompiled.cpp:3-36) lays out layer 0 */
+  uint64_t offs = 0;
+  for(uint32_t m = 0; m < mip; m++)
+  {
+    uint32_t mw = t->width >> m, mh = t->height >> m;
+    if(mw < 1) mw = 1;
+    if(mh < 1) mh = 1;
+    offs += (uint64_t)mw * mh * 4;
+  }
+  return offs;
+}
+
+static void build_mips(vsc_texture *t)
+{
+  for(uint32_t m = 1; m < t->mips; m++)
+  {
+    uint32_t pw = t->width >> (m - 1), ph = t->height >> (m - 1);
+    uint32_t mw = t->width >> m, mh = t->height >> m;
+    if(pw < 1) pw = 1;
+    if(ph < 1) ph = 1;
+    if(mw < 1) mw = 1;
+    if(mh < 1) mh = 1;
+    const uint8_t *src = t->texels + vsc_texture_mip_offset(t, m - 1);
+    uint8_t *dst = t->texels + vsc_texture_mip_offset(t, m);
+    for(uint32_t y = 0; y < mh; y++)
+      for(uint32_t x = 0; x < mw; x++)
+      {
+        uint32_t x0 = 2 * x, y0 = 2 * y;
+        uint32_t x1 = x0 + 1 < pw ? x0 + 1 : x0, y1 = y0 + 1 < ph ? y0 + 1 : y0;
+        for(int c = 0; c < 4; c++)
+        {
+          uint32_t sum = src[(y0 * pw + x0) * 4 + c] + src[(y0 * pw + x1) * 4 + c] +
+                         src[(y1 * pw + x0) * 4 + c] + src[(y1 * pw + x1) * 4 + c];
+          dst[(y * mw + x) * 4 + c] = (uint8_t)((sum + 2) >> 2);
+        }
+      }
+  }
+}
+
+static uint32_t add_texture_id(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
+                               const uint8_t *texels, uint64_t seed, uint64_t id);
+
+uint32_t vsc_add_texture(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
+                         const uint8_t *texels, uint64_t seed)
+{
+  return add_texture_id(s, width, height, mips, texels, seed, s->num_textures);
+}
+
+/* Texture contents depend only on (seed, id), so a texture pool is the same in every scene. */
+static uint32_t add_texture_id(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
+                               const uint8_t *texels, uint64_t seed, uint64_t id)
+{
+  uint64_t cap = s->cap_textures;
+  GROW(s->textures, cap, (uint64_t)s->num_textures + 1, vsc_texture);
+  s->cap_textures = (uint32_t)cap;
+  vsc_texture *t = &s->textures[s->num_textures];
+  t->width = width;
+  t->height = height;
+  t->mips = mips ? mips : 1;
+  t->bytes = vsc_texture_mip_offset(t, t->mips);
+  t->texels = (uint8_t *)malloc((size_t)t->bytes);
+  uint64_t mip0 = (uint64_t)width * height * 4;
+  if(texels)
+  {
+    memcpy(t->texels, texels, (size_t)mip0);
+  }
+  else
+  {
+    rng r = rng_for(seed, 0xfe, id);
+    for(uint64_t i = 0; i < mip0; i += 4)
+    {
+      uint32_t v = urand_u32(&r);
+      memcpy(t->texels + i, &v, 4);
+    }
+  }
+  build_mips(t);
+  return s->num_textures++;
+}
+
+uint64_t vsc_add_vertices(vsc_scene *s, const void *data, uint64_t bytes)
+{
+  uint64_t offs = s->vb_bytes;
+  GROW(s->vb, s->cap_vb, offs + bytes, uint8_t);
+  memcpy(s->vb + offs, data, (size_t)bytes);
+  s->vb_bytes = offs + bytes;
+  return offs;
+}
+
+uint64_t vsc_add_indices(vsc_scene *s, const uint32_t *idx, uint64_t count)
+{
+  uint64_t first = s->ib_count;
+  GROW(s->ib, s->cap_ib, first + count, uint32_t);
+  memcpy(s->ib + first, idx, (size_t)(count * 4));
+  s->ib_count = first + count;
+  return first;
+}
+
+static uint8_t *reserve_vertices(vsc_scene *s, uint64_t bytes, uint64_t *offs)
+{
+  *offs = s->vb_bytes;
+  GROW(s->vb, s->cap_vb, s->vb_bytes + bytes, uint8_t);
+  s->vb_bytes += bytes;
+  return s->vb + *offs;
+}
+
+static uint32_t *reserve_indices(vsc_scene *s, uint64_t count, uint64_t *first)
+{
+  *first = s->ib_count;
+  GROW(s->ib, s->cap_ib, s->ib_count + count, uint32_t);
+  s->ib_count += count;
+  return s->ib + *first;
+}
+
+uint32_t vsc_add_draw(vsc_scene *s, const vsc_draw *d)
+{
+  uint64_t cap = s->cap_draws;
+  GROW(s->draws, cap, (uint64_t)s->num_draws + 1, vsc_draw);
+  s->cap_draws = (uint32_t)cap;
+  s->draws[s->num_draws] = *d;
+  return s->num_draws++;
+}
+
+uint32_t vsc_add_pass(vsc_scene *s, uint32_t target, uint32_t clear, uint32_t first_draw,
+                      uint32_t draw_count)
+{
+  uint64_t cap = s->cap_passes;
+  GROW(s->passes, cap, (uint64_t)s->num_passes + 1, vsc_pass);
+  s->cap_passes = (uint32_t)cap;
+  vsc_pass *p = &s->passes[s->num_passes];
+  p->target = target;
+  p->clear = clear;
+  p->first_draw = first_draw;
+  p->draw_count = draw_count;
+  return s->num_passes++;
+}
+
+uint32_t vsc_stride_of(uint32_t shader)
+{
+  switch(shader)
+  {
+    case VSC_SHADER_LAMBERT_TEX: return VSC_STRIDE_LAMBERT_TEX;
+    case VSC_SHADER_COLOR: return VSC_STRIDE_COLOR;
+    case VSC_SHADER_LAMBERT_TEX_ALPHA: return VSC_STRIDE_LAMBERT_TEX_ALPHA;
+    default: return 0;
+  }
+}
+
+uint32_t vsc_vertex_attrs(uint32_t shader, vsc_attr *a)
+{
+  switch(shader)
+  {
+    case VSC_SHADER_LAMBERT_TEX:
+    case VSC_SHADER_LAMBERT_TEX_ALPHA:
+      a[0].location = 0; a[0].format = 106; a[0].offset = 0;  /* position */
+      a[1].location = 1; a[1].format = 106; a[1].offset = 12; /* normal */
+      a[2].location = 2; a[2].format = 103; a[2].offset = 24; /* uv */
+      if(shader == VSC_SHADER_LAMBERT_TEX)
+        return 3;
+      a[3].location = 3; a[3].format = 100; a[3].offset = 32; /* alpha */
+      return 4;
+    case VSC_SHADER_COLOR:
+      a[0].location = 0; a[0].format = 109; a[0].offset = 0;  /* clip-space position */
+      a[1].location = 1; a[1].format = 37; a[1].offset = 16;  /* RGBA8 colour */
+      return 2;
+    default: return 0;
+  }
+}
+
+uint64_t vsc_triangle_count(const vsc_scene *s)
+{
+  uint64_t n = 0;
+  for(uint32_t i = 0; i < s->num_draws; i++)
+  {
+    const vsc_draw *d = &s->draws[i];
+    const vsc_pipeline *p = &s->pipelines[d->pipeline];
+    if(p->topology == VSC_TOPOLOGY_TRIANGLE_STRIP)
+      n += d->count >= 3 ? d->count - 2 : 0;
+    else
+      n += d->count / 3;
+  }
+  return n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* matrices (double, column-major m[c*4+r]) and meshes                       */
+/* ------------------------------------------------------------------------ */
+
+static void mat_mul(const double *a, const double *b, double *out)
+{
+  double t[16];
+  for(int c = 0; c < 4; c++)
+    for(int r = 0; r < 4; r++)
+    {
+      double acc = 0.0;
+      for(int k = 0; k < 4; k++)
+        acc = acc + a[k * 4 + r] * b[c * 4 + k];
+      t[c * 4 + r] = acc;
+    }
+  memcpy(out, t, sizeof(t));
+}
+
+static void mat_perspective(double aspect, double near, double far, double *m)
+{
+  /* fov 60 degrees: 1/tan(30 deg) = sqrt(3); depth maps [-near,-far] -> [0,1] */
+  double f = sqrt(3.0);
+  memset(m, 0, 16 * sizeof(double));
+  m[0] = f / aspect;
+  m[5] = f;
+  m[10] = far / (near - far);
+  m[11] = -1.0;
+  m[14] = near * far / (near - far);
+}
+
+/* translation * rotation(quaternion from three uniforms) * uniform scale */
+static void mat_model(rng *r, double tx, double ty, double tz, double scale, double *m)
+{
+  double u1 = urand(r), u2 = urand(r), u3 = urand(r);
+  double a = sqrt(1.0 - u1), b = sqrt(u1);
+  double qx = a * vsc_sin(2.0 * kPi * u2), qy = a * vsc_cos(2.0 * kPi * u2);
+  double qz = b * vsc_sin(2.0 * kPi * u3), qw = b * vsc_cos(2.0 * kPi * u3);
+  double R[9] = {
+      1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy + qz * qw),     2 * (qx * qz - qy * qw),
+      2 * (qx * qy - qz * qw),     1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz + qx * qw),
+      2 * (qx * qz + qy * qw),     2 * (qy * qz - qx * qw),     1 - 2 * (qx * qx + qy * qy),
+  };
+  memset(m, 0, 16 * sizeof(double));
+  for(int c = 0; c < 3; c++)
+    for(int rr = 0; rr < 3; rr++)
+      m[c * 4 + rr] = R[c * 3 + rr] * scale;
+  m[12] = tx;
+  m[13] = ty;
+  m[14] = tz;
+  m[15] = 1.0;
+}
+
+static void write_mvp_push(vsc_draw *d, const double *mvp, const double *light)
+{
+  float f[20];
+  for(int i = 0; i < 16; i++)
+    f[i] = (float)mvp[i];
+  for(int i = 0; i < 4; i++)
+    f[16 + i] = (float)light[i];
+  memcpy(d->push, f, sizeof(f));
+  d->push_size = sizeof(f);
+}
+
+static void random_light(rng *r, double *l)
+{
+  /* unit vector biased toward +z so most of a mesh is lit */
+  double x = urand(r) * 2.0 - 1.0, y = urand(r) * 2.0 - 1.0, z = urand(r) * 0.8 + 0.6;
+  double len = sqrt(x * x + y * y + z * z);
+  l[0] = x / len;
+  l[1] = y / len;
+  l[2] = z / len;
+  l[3] = 0.0;
+}
+
+typedef struct mesh_out {
+  uint64_t vb_offset; /* bytes */
+  uint64_t first_index;
+  uint32_t index_count;
+} mesh_out;
+
+static void put_vertex(uint8_t *dst, uint32_t stride, const double *pos, const double *nrm,
+                       const double *uv, double alpha)
+{
+  float f[9];
+  for(int i = 0; i < 3; i++)
+    f[i] = (float)pos[i];
+  for(int i = 0; i < 3; i++)
+    f[3 + i] = (float)nrm[i];
+  f[6] = (float)uv[0];
+  f[7] = (float)uv[1];
+  f[8] = (float)alpha;
+  memcpy(dst, f, stride);
+}
+
+/* Quad grid connectivity shared by spheres and sheets: (cols x rows) quads. */
+static void grid_indices(uint32_t *ib, uint32_t cols, uint32_t rows)
+{
+  uint32_t k = 0;
+  for(uint32_t j = 0; j < rows; j++)
+    for(uint32_t i = 0; i < cols; i++)
+    {
+      uint32_t a = j * (cols + 1) + i, b = a + cols + 1, c = b + 1, d = a + 1;
+      ib[k++] = a;
+      ib[k++] = b;
+      ib[k++] = d;
+      ib[k++] = d;
+      ib[k++] = b;
+      ib[k++] = c;
+    }
+}
+
+/* UV sphere of radius 1 with optional smooth displacement; nlon x nlat quads. */
+static mesh_out make_sphere(vsc_scene *s, uint32_t nlon, uint32_t nlat, double amp, rng *r,
+                            uint32_t stride, double alpha_lo, double alpha_hi)
+{
+  mesh_out m;
+  uint64_t nv = (uint64_t)(nlon + 1) * (nlat + 1);
+  double fa = 1.0 + (double)(urand_u32(r) % 5), fb = 2.0 * kPi * urand(r);
+  double fc = 1.0 + (double)(urand_u32(r) % 6), fd = 2.0 * kPi * urand(r);
+  uint8_t *vb = reserve_vertices(s, nv * stride, &m.vb_offset);
+  for(uint32_t j = 0; j <= nlat; j++)
+  {
+    double th = kPi * (double)j / (double)nlat;
+    double st = vsc_sin(th), ct = vsc_cos(th);
+    for(uint32_t i = 0; i <= nlon; i++)
+    {
+      double ph = 2.0 * kPi * (double)i / (double)nlon;
+      double sp = vsc_sin(ph), cp = vsc_cos(ph);
+      double rad = 1.0 + amp * vsc_sin(fa * th + fb) * vsc_cos(fc * ph + fd);
+      double n[3] = {st * cp, ct, st * sp};
+      double p[3] = {n[0] * rad, n[1] * rad, n[2] * rad};
+      double uv[2] = {(double)i / (double)nlon, (double)j / (double)nlat};
+      double alpha = alpha_lo + (alpha_hi - alpha_lo) * urand(r);
+      put_vertex(vb + ((uint64_t)j * (nlon + 1) + i) * stride, stride, p, n, uv, alpha);
+    }
+  }
+  m.index_count = nlon * nlat * 6;
+  uint32_t *ib = reserve_indices(s, m.index_count, &m.first_index);
+  grid_indices(ib, nlon, nlat);
+  return m;
+}
+
+/* Displaced sheet in [-1,1]^2, nx x ny quads. */
+static mesh_out make_sheet(vsc_scene *s, uint32_t nx, uint32_t ny, rng *r, uint32_t stride)
+{
+  mesh_out m;
+  uint64_t nv = (uint64_t)(nx + 1) * (ny + 1);
+  double fa = 1.0 + 3.0 * urand(r), fb = 1.0 + 3.0 * urand(r), ph = 2.0 * kPi * urand(r);
+  uint8_t *vb = reserve_vertices(s, nv * stride, &m.vb_offset);
+  for(uint32_t j = 0; j <= ny; j++)
+    for(uint32_t i = 0; i <= nx; i++)
+    {
+      double u = (double)i / (double)nx, v = (double)j / (double)ny;
+      double x = u * 2.0 - 1.0, y = v * 2.0 - 1.0;
+      double z = 0.25 * vsc_sin(fa * x * kPi + ph) * vsc_cos(fb * y * kPi);
+      double dzdx = 0.25 * fa * kPi * vsc_cos(fa * x * kPi + ph) * vsc_cos(fb * y * kPi);
+      double dzdy = -0.25 * fb * kPi * vsc_sin(fa * x * kPi + ph) * vsc_sin(fb * y * kPi);
+      double n[3] = {-dzdx, -dzdy, 1.0};
+      double len = sqrt(n[0] * n[0] + n[1] * n[1] + 1.0);
+      n[0] /= len;
+      n[1] /= len;
+      n[2] /= len;
+      double p[3] = {x, y, z};
+      double uv[2] = {u, v};
+      put_vertex(vb + ((uint64_t)j * (nx + 1) + i) * stride, stride, p, n, uv, 1.0);
+    }
+  m.index_count = nx * ny * 6;
+  uint32_t *ib = reserve_indices(s, m.index_count, &m.first_index);
+  grid_indices(ib, nx, ny);
+  return m;
+}
+
+/* Pick quad-grid dimensions giving about `tris` triangles. */
+static void grid_dims(double tris, uint32_t *cols, uint32_t *rows)
+{
+  double quads = tris * 0.5;
+  uint32_t r = (uint32_t)round_det(sqrt(quads * 0.5));
+  if(r < 2) r = 2;
+  uint32_t c = (uint32_t)round_det(quads / (double)r);
+  if(c < 3) c = 3;
+  *cols = c;
+  *rows = r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* configurations                                                            */
+/* ------------------------------------------------------------------------ */
+
+static vsc_pipeline pipe_defaults(uint32_t shader, uint32_t flags)
+{
+  vsc_pipeline p;
+  memset(&p, 0, sizeof(p));
+  p.shader = shader;
+  p.topology = VSC_TOPOLOGY_TRIANGLE_LIST;
+  p.cull_mode = (flags & VSC_FLAG_BACKFACE_CULL) ? VSC_CULL_BACK : VSC_CULL_NONE;
+  p.front_face = (flags & VSC_FLAG_CLOCKWISE) ? VSC_FRONT_CW : VSC_FRONT_CCW;
+  p.depth_test = 1;
+  p.depth_op = VSC_CMP_LESS;
+  p.depth_write = 1;
+  p.blend_enable = 0;
+  p.src_factor = VSC_BLEND_ONE;
+  p.dst_factor = VSC_BLEND_ZERO;
+  p.filter = VSC_FILTER_REFERENCE;
+  return p;
+}
+
+#define PARAM(field, dflt) ((params && params->field) ? params->field : (dflt))
+
+/* cfg1: 512x512, one UV sphere (64 lon x 32 lat) per frame, one frame per target. */
+static void gen_sphere(vsc_scene *s, uint64_t seed, const vsc_params *params)
+{
+  uint32_t w = PARAM(width, 512), h = PARAM(height, 512), frames = PARAM(count, 1);
+  uint32_t flags = params ? params->flags : 0;
+  vsc_pipeline p = pipe_defaults(VSC_SHADER_LAMBERT_TEX, flags);
+  uint32_t pipe = vsc_add_pipeline(s, &p);
+  uint32_t tsz = PARAM(tex_size, 256);
+  uint32_t tex = vsc_add_texture(s, tsz, tsz, 1, NULL, seed);
+  rng mr = rng_for(seed, 1, 0);
+  mesh_out m = make_sphere(s, 64, 32, 0.0, &mr, VSC_STRIDE_LAMBERT_TEX, 1.0, 1.0);
+  double P[16];
+  mat_perspective((double)w / (double)h, 0.1, 100.0, P);
+  for(uint32_t f = 0; f < frames; f++)
+  {
+    rng r = rng_for(seed, 1, 1000 + f);
+    double M[16], MVP[16], L[4];
+    mat_model(&r, 0.0, 0.0, -3.0, 1.0, M);
+    mat_mul(P, M, MVP);
+    random_light(&r, L);
+    vsc_draw d;
+    memset(&d, 0, sizeof(d));
+    d.pipeline = pipe;
+    d.texture = tex;
+    d.indexed = 1;
+    d.count = m.index_count;
+    d.first = (uint32_t)m.first_index;
+    d.vb_offset = m.vb_offset;
+    write_mvp_push(&d, MVP, L);
+    uint32_t t = vsc_add_target(s, w, h);
+    uint32_t di = vsc_add_draw(s, &d);
+    vsc_add_pass(s, t, 1, di, 1);
+  }
+}
+
+/* cfg2: 1920x1080, N screen-space triangles, log-uniform area, alpha blended. */
+static void gen_tris(vsc_scene *s, uint64_t seed, const vsc_params *params)
+{
+  uint32_t w = PARAM(width, 1920), h = PARAM(height, 1080), n = PARAM(count, 1000000);
+  double max_area = (params && params->max_area > 0.0f) ? (double)params->max_area : 10000.0;
+  uint32_t flags = params ? params->flags : 0;
+  vsc_pipeline p = pipe_defaults(VSC_SHADER_COLOR, flags);
+  p.depth_op = VSC_CMP_LEQUAL;
+  if(!(flags & VSC_FLAG_NO_BLEND))
+  {
+    p.blend_enable = 1;
+    p.src_factor = VSC_BLEND_SRC_ALPHA;
+    p.dst_factor = VSC_BLEND_ONE_MINUS_SRC_ALPHA;
+  }
+  uint32_t pipe = vsc_add_pipeline(s, &p);
+  uint64_t offs = 0;
+  uint8_t *vb = reserve_vertices(s, (uint64_t)n * 3 * VSC_STRIDE_COLOR, &offs);
+  const double k = 4.0 / (3.0 * sqrt(3.0)); /* circumradius^2 of an equilateral triangle per area */
+  for(uint32_t t = 0; t < n; t++)
+  {
+    rng r = rng_for(seed, 2, t);
+    double cx = urand(&r) * (double)w, cy = urand(&r) * (double)h;
+    double area = loguniform(&r, 1.0, max_area > 1.0 ? max_area : 1.0001);
+    double rad = sqrt(k * area), th = 2.0 * kPi * urand(&r);
+    for(int v = 0; v < 3; v++)
+    {
+      double a = th + (double)v * (2.0 * kPi / 3.0);
+      double px = cx + rad * vsc_cos(a), py = cy + rad * vsc_sin(a);
+      float f[4];
+      f[0] = (float)(px / (double)w * 2.0 - 1.0);
+      f[1] = (float)(1.0 - py / (double)h * 2.0);
+      f[2] = (float)urand(&r);
+      f[3] = 1.0f;
+      uint8_t col[4];
+      col[0] = (uint8_t)(urand_u32(&r) & 0xff);
+      col[1] = (uint8_t)(urand_u32(&r) & 0xff);
+      col[2] = (uint8_t)(urand_u32(&r) & 0xff);
+      col[3] = (uint8_t)(51 + urand_u32(&r) % 205); /* alpha in [0.2, 1] */
+      uint8_t *dst = vb + ((uint64_t)t * 3 + v) * VSC_STRIDE_COLOR;
+      memcpy(dst, f, 16);
+      memcpy(dst + 16, col, 4);
+    }
+  }
+  vsc_draw d;
+  memset(&d, 0, sizeof(d));
+  d.pipeline = pipe;
+  d.texture = VSC_NONE;
+  d.indexed = 0;
+  d.count = n * 3;
+  d.first = 0;
+  d.vb_offset = offs;
+  uint32_t tgt = vsc_add_target(s, w, h);
+  uint32_t di = vsc_add_draw(s, &d);
+  vsc_add_pass(s, tgt, 1, di, 1);
+}
+
+/* Place an object of radius `radius` fully in front of the camera, inside the frustum. */
+static void place_object(rng *r, double aspect, double *P, double radius_lo, double radius_hi,
+                         double *mvp)
+{
+  double dist = loguniform(r, 4.0, 40.0);
+  double half = dist / sqrt(3.0); /* tan(30 deg) * dist */
+  double x = (urand(r) * 2.0 - 1.0) * half * aspect * 0.9;
+  double y = (urand(r) * 2.0 - 1.0) * half * 0.9;
+  double rad = dist * (radius_lo + (radius_hi - radius_lo) * urand(r));
+  double M[16];
+  mat_model(r, x, y, -dist, rad, M);
+  mat_mul(P, M, mvp);
+}
+
+/* cfg3: 2560x1440, many indexed draws of uneven size into one target. */
+static void gen_draws(vsc_scene *s, uint64_t seed, const vsc_params *params)
+{
+  uint32_t w = PARAM(width, 2560), h = PARAM(height, 1440), n = PARAM(count, 10000);
+  uint32_t lo = PARAM(min_tris, 12), hi = PARAM(max_tris, 50000);
+  uint32_t ntex = PARAM(textures, 64), tsz = PARAM(tex_size, 512);
+  uint32_t flags = params ? params->flags : 0;
+  vsc_pipeline p = pipe_defaults(VSC_SHADER_LAMBERT_TEX, flags);
+  p.filter = (flags & VSC_FLAG_FILTER_REFERENCE) ? VSC_FILTER_REFERENCE : VSC_FILTER_TRILINEAR;
+  uint32_t pipe = vsc_add_pipeline(s, &p);
+  uint32_t mips = 1;
+  while((tsz >> mips) > 0)
+    mips++;
+  for(uint32_t t = 0; t < ntex; t++)
+    vsc_add_texture(s, tsz, tsz, mips, NULL, seed);
+  double P[16];
+  mat_perspective((double)w / (double)h, 0.1, 100.0, P);
+  uint32_t tgt = vsc_add_target(s, w, h);
+  uint32_t first = s->num_draws;
+  for(uint32_t i = 0; i < n; i++)
+  {
+    rng r = rng_for(seed, 3, i);
+    double tris = loguniform(&r, (double)lo, (double)(hi > lo ? hi : lo + 1));
+    uint32_t cols, rows;
+    grid_dims(tris, &cols, &rows);
+    mesh_out m;
+    if(urand(&r) < 0.5)
+      m = make_sphere(s, cols, rows, 0.15, &r, VSC_STRIDE_LAMBERT_TEX, 1.0, 1.0);
+    else
+      m = make_sheet(s, cols, rows, &r, VSC_STRIDE_LAMBERT_TEX);
+    double MVP[16], L[4];
+    place_object(&r, (double)w / (double)h, P, 0.01, 0.1, MVP);
+    random_light(&r, L);
+    vsc_draw d;
+    memset(&d, 0, sizeof(d));
+    d.pipeline = pipe;
+    d.texture = urand_u32(&r) % ntex;
+    d.indexed = 1;
+    d.count = m.index_count;
+    d.first = (uint32_t)m.first_index;
+    d.vb_offset = m.vb_offset;
+    write_mvp_push(&d, MVP, L);
+    vsc_add_draw(s, &d);
+  }
+  vsc_add_pass(s, tgt, 1, first, n);
+}
+
+/* cfg4: many small independent targets, one mesh each, even targets alpha blended. */
+static void gen_targets(vsc_scene *s, uint64_t seed, const vsc_params *params)
+{
+  uint32_t w = PARAM(width, 128), h = PARAM(height, 128), n = PARAM(count, 1024);
+  uint32_t lo = PARAM(min_tris, 500), hi = PARAM(max_tris, 20000);
+  uint32_t ntex = PARAM(textures, 16), tsz = PARAM(tex_size, 256);
+  uint32_t flags = params ? params->flags : 0;
+  vsc_pipeline opaque = pipe_defaults(VSC_SHADER_LAMBERT_TEX_ALPHA, flags);
+  vsc_pipeline blended = opaque;
+  if(!(flags & VSC_FLAG_NO_BLEND))
+  {
+    blended.blend_enable = 1;
+    blended.src_factor = VSC_BLEND_SRC_ALPHA;
+    blended.dst_factor = VSC_BLEND_ONE_MINUS_SRC_ALPHA;
+  }
+  uint32_t p_opaque = vsc_add_pipeline(s, &opaque);
+  uint32_t p_blend = vsc_add_pipeline(s, &blended);
+  uint32_t mips = 1;
+  while((tsz >> mips) > 0)
+    mips++;
+  for(uint32_t t = 0; t < ntex; t++)
+    vsc_add_texture(s, tsz, tsz, mips, NULL, seed);
+  double P[16];
+  mat_perspective((double)w / (double)h, 0.1, 100.0, P);
+  for(uint32_t i = 0; i < n; i++)
+  {
+    rng r = rng_for(seed, 4, i);
+    double tris = loguniform(&r, (double)lo, (double)(hi > lo ? hi : lo + 1));
+    uint32_t cols, rows;
+    grid_dims(tris, &cols, &rows);
+    int blend = (i % 2) == 0;
+    mesh_out m = make_sphere(s, cols, rows, 0.1, &r, VSC_STRIDE_LAMBERT_TEX_ALPHA,
+                             blend ? 0.3 : 1.0, 1.0);
+    double M[16], MVP[16], L[4];
+    mat_model(&r, 0.0, 0.0, -3.0, 1.0, M);
+    mat_mul(P, M, MVP);
+    random_light(&r, L);
+    vsc_draw d;
+    memset(&d, 0, sizeof(d));
+    d.pipeline = blend ? p_blend : p_opaque;
+    d.texture = urand_u32(&r) % ntex;
+    d.indexed = 1;
+    d.count = m.index_count;
+    d.first = (uint32_t)m.first_index;
+    d.vb_offset = m.vb_offset;
+    write_mvp_push(&d, MVP, L);
+    uint32_t tgt = vsc_add_target(s, w, h);
+    uint32_t di = vsc_add_draw(s, &d);
+    vsc_add_pass(s, tgt, 1, di, 1);
+  }
+}
+
+/* cfg5: one serving request; params->count is the request index. */
+static void gen_request(vsc_scene *s, uint64_t seed, const vsc_params *params)
+{
+  static const uint32_t res[4][2] = {{256, 256}, {512, 512}, {1024, 1024}, {1920, 1080}};
+  uint32_t idx = params ? params->count : 0;
+  uint32_t lo = PARAM(min_tris, 1000), hi = PARAM(max_tris, 2000000);
+  uint32_t ntex = PARAM(textures, 32), tsz = PARAM(tex_size, 1024);
+  uint32_t flags = params ? params->flags : 0;
+  rng r = rng_for(seed, 5, idx);
+  uint32_t pick = urand_u32(&r) % 4;
+  uint32_t w = PARAM(width, res[pick][0]), h = PARAM(height, res[pick][1]);
+  vsc_pipeline p = pipe_defaults(VSC_SHADER_LAMBERT_TEX, flags);
+  p.filter = (flags & VSC_FLAG_FILTER_REFERENCE) ? VSC_FILTER_REFERENCE : VSC_FILTER_TRILINEAR;
+  uint32_t pipe = vsc_add_pipeline(s, &p);
+  uint32_t mips = 1;
+  while((tsz >> mips) > 0)
+    mips++;
+  uint32_t texid = urand_u32(&r) % ntex;
+  /* the texture a request binds is the same seeded texture whichever request uses it */
+  add_texture_id(s, tsz, tsz, mips, NULL, seed, texid);
+  double tris = loguniform(&r, (double)lo, (double)(hi > lo ? hi : lo + 1));
+  uint32_t cols, rows;
+  grid_dims(tris, &cols, &rows);
+  mesh_out m = make_sphere(s, cols, rows, 0.1, &r, VSC_STRIDE_LAMBERT_TEX, 1.0, 1.0);
+  double P[16], M[16], MVP[16], L[4];
+  mat_perspective((double)w / (double)h, 0.1, 100.0, P);
+  mat_model(&r, 0.0, 0.0, -2.5 - urand(&r), 1.0, M);
+  mat_mul(P, M, MVP);
+  random_light(&r, L);
+  vsc_draw d;
+  memset(&d, 0, sizeof(d));
+  d.pipeline = pipe;
+  d.texture = 0;
+  d.indexed = 1;
+  d.count = m.index_count;
+  d.first = (uint32_t)m.first_index;
+  d.vb_offset = m.vb_offset;
+  write_mvp_push(&d, MVP, L);
+  uint32_t tgt = vsc_add_target(s, w, h);
+  uint32_t di = vsc_add_draw(s, &d);
+  vsc_add_pass(s, tgt, 1, di, 1);
+}
+
+int vsc_generate(uint32_t config, uint64_t seed, const vsc_params *params, vsc_scene **out)
+{
+  vsc_scene *s = vsc_new();
+  s->config = config;
+  s->seed = seed;
+  switch(config)
+  {
+    case VSC_CFG_SPHERE: gen_sphere(s, seed, params); break;
+    case VSC_CFG_TRIS: gen_tris(s, seed, params); break;
+    case VSC_CFG_DRAWS: gen_draws(s, seed, params); break;
+    case VSC_CFG_TARGETS: gen_targets(s, seed, params); break;
+    case VSC_CFG_SERVING: gen_request(s, seed, params); break;
+    default: vsc_free(s); *out = NULL; return -1;
+  }
+  *out = s;
+  return 0;
+}

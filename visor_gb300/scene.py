@@ -1,0 +1,201 @@
+"""ctypes mirror of include/visor_scene.h (seeded synthetic scenes).
+
+The generator itself is C (visor_gb300/csrc/scene/scene.c) and is linked into
+the product library; every consumer (GPU path, CPU oracle, reference build)
+gets byte-identical scenes from it.
+"""
+import ctypes as C
+
+import numpy as np
+
+SHADER_LAMBERT_TEX = 1
+SHADER_COLOR = 2
+SHADER_LAMBERT_TEX_ALPHA = 3
+
+FILTER_REFERENCE = 0
+FILTER_TRILINEAR = 1
+FILTER_NEAREST = 2
+
+CULL_NONE, CULL_FRONT, CULL_BACK, CULL_FRONT_AND_BACK = 0, 1, 2, 3
+FRONT_CCW, FRONT_CW = 0, 1
+CMP_NEVER, CMP_LESS, CMP_EQUAL, CMP_LEQUAL, CMP_GREATER, CMP_NOT_EQUAL, CMP_GEQUAL, CMP_ALWAYS = range(8)
+BLEND_ZERO, BLEND_ONE, BLEND_SRC_ALPHA, BLEND_ONE_MINUS_SRC_ALPHA = 0, 1, 6, 7
+TOPOLOGY_TRIANGLE_LIST, TOPOLOGY_TRIANGLE_STRIP = 3, 4
+
+CFG_SPHERE, CFG_TRIS, CFG_DRAWS, CFG_TARGETS, CFG_SERVING = 1, 2, 3, 4, 5
+
+FLAG_BACKFACE_CULL = 1 << 0
+FLAG_NO_BLEND = 1 << 1
+FLAG_FILTER_REFERENCE = 1 << 2
+FLAG_CLOCKWISE = 1 << 3
+
+NONE = 0xFFFFFFFF
+
+
+class Pipeline(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in (
+        "shader", "topology", "cull_mode", "front_face", "depth_test", "depth_op", "depth_write",
+        "blend_enable", "src_factor", "dst_factor", "filter")]
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("mips", C.c_uint32),
+                ("bytes", C.c_uint64), ("texels", C.POINTER(C.c_uint8))]
+
+
+class Target(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class Draw(C.Structure):
+    _fields_ = [("pipeline", C.c_uint32), ("texture", C.c_uint32), ("indexed", C.c_uint32),
+                ("count", C.c_uint32), ("first", C.c_uint32), ("push_size", C.c_uint32),
+                ("vb_offset", C.c_uint64), ("push", C.c_uint8 * 128)]
+
+
+class Pass(C.Structure):
+    _fields_ = [("target", C.c_uint32), ("clear", C.c_uint32), ("first_draw", C.c_uint32),
+                ("draw_count", C.c_uint32)]
+
+
+class Scene(C.Structure):
+    _fields_ = [
+        ("config", C.c_uint32), ("seed", C.c_uint64), ("clear_color", C.c_float * 4),
+        ("clear_depth", C.c_float),
+        ("num_targets", C.c_uint32), ("targets", C.POINTER(Target)),
+        ("num_pipelines", C.c_uint32), ("pipelines", C.POINTER(Pipeline)),
+        ("num_textures", C.c_uint32), ("textures", C.POINTER(Texture)),
+        ("vb_bytes", C.c_uint64), ("vb", C.POINTER(C.c_uint8)),
+        ("ib_count", C.c_uint64), ("ib", C.POINTER(C.c_uint32)),
+        ("num_draws", C.c_uint32), ("draws", C.POINTER(Draw)),
+        ("num_passes", C.c_uint32), ("passes", C.POINTER(Pass)),
+        ("cap_targets", C.c_uint32), ("cap_pipelines", C.c_uint32), ("cap_textures", C.c_uint32),
+        ("cap_draws", C.c_uint32), ("cap_passes", C.c_uint32),
+        ("cap_vb", C.c_uint64), ("cap_ib", C.c_uint64),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("count", C.c_uint32),
+                ("min_tris", C.c_uint32), ("max_tris", C.c_uint32), ("max_area", C.c_float),
+                ("flags", C.c_uint32), ("textures", C.c_uint32), ("tex_size", C.c_uint32)]
+
+
+def bind_scene_api(lib):
+    """Declare the vsc_* signatures on a library that links scene.c."""
+    SP = C.POINTER(Scene)
+    lib.vsc_generate.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(Params), C.POINTER(SP)]
+    lib.vsc_generate.restype = C.c_int
+    lib.vsc_new.argtypes = []
+    lib.vsc_new.restype = SP
+    lib.vsc_free.argtypes = [SP]
+    lib.vsc_free.restype = None
+    lib.vsc_add_target.argtypes = [SP, C.c_uint32, C.c_uint32]
+    lib.vsc_add_target.restype = C.c_uint32
+    lib.vsc_add_pipeline.argtypes = [SP, C.POINTER(Pipeline)]
+    lib.vsc_add_pipeline.restype = C.c_uint32
+    lib.vsc_add_texture.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64]
+    lib.vsc_add_texture.restype = C.c_uint32
+    lib.vsc_add_vertices.argtypes = [SP, C.c_void_p, C.c_uint64]
+    lib.vsc_add_vertices.restype = C.c_uint64
+    lib.vsc_add_indices.argtypes = [SP, C.c_void_p, C.c_uint64]
+    lib.vsc_add_indices.restype = C.c_uint64
+    lib.vsc_add_draw.argtypes = [SP, C.POINTER(Draw)]
+    lib.vsc_add_draw.restype = C.c_uint32
+    lib.vsc_add_pass.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
+    lib.vsc_add_pass.restype = C.c_uint32
+    lib.vsc_triangle_count.argtypes = [SP]
+    lib.vsc_triangle_count.restype = C.c_uint64
+    lib.vsc_hash_bytes.argtypes = [C.c_void_p, C.c_uint64]
+    lib.vsc_hash_bytes.restype = C.c_uint64
+    return lib
+
+
+class SceneHandle:
+    """Owns a vsc_scene* created by `lib` and frees it with the same library."""
+
+    def __init__(self, lib, ptr):
+        self.lib = lib
+        self.ptr = ptr
+
+    @property
+    def s(self):
+        return self.ptr.contents
+
+    def targets(self):
+        s = self.s
+        return [(s.targets[i].width, s.targets[i].height) for i in range(s.num_targets)]
+
+    def triangle_count(self):
+        return int(self.lib.vsc_triangle_count(self.ptr))
+
+    def close(self):
+        if self.ptr:
+            self.lib.vsc_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def generate(lib, config, seed, **params):
+    p = Params()
+    for k, v in params.items():
+        setattr(p, k, v)
+    out = C.POINTER(Scene)()
+    rc = lib.vsc_generate(config, seed, C.byref(p), C.byref(out))
+    if rc != 0:
+        raise ValueError(f"vsc_generate({config}) failed: {rc}")
+    return SceneHandle(lib, out)
+
+
+def new_scene(lib):
+    return SceneHandle(lib, lib.vsc_new())
+
+
+def make_pipeline(shader, **kw):
+    p = Pipeline()
+    p.shader = shader
+    p.topology = kw.get("topology", TOPOLOGY_TRIANGLE_LIST)
+    p.cull_mode = kw.get("cull_mode", CULL_NONE)
+    p.front_face = kw.get("front_face", FRONT_CCW)
+    p.depth_test = kw.get("depth_test", 1)
+    p.depth_op = kw.get("depth_op", CMP_LESS)
+    p.depth_write = kw.get("depth_write", 1)
+    p.blend_enable = kw.get("blend_enable", 0)
+    p.src_factor = kw.get("src_factor", BLEND_ONE)
+    p.dst_factor = kw.get("dst_factor", BLEND_ZERO)
+    p.filter = kw.get("filter", FILTER_REFERENCE)
+    return p
+
+
+def make_draw(pipeline, count, first=0, indexed=False, texture=NONE, vb_offset=0, push=b""):
+    d = Draw()
+    d.pipeline = pipeline
+    d.texture = texture
+    d.indexed = 1 if indexed else 0
+    d.count = count
+    d.first = first
+    d.vb_offset = vb_offset
+    d.push_size = len(push)
+    C.memmove(d.push, push, len(push))
+    return d
+
+
+def target_buffers(handle):
+    """Allocate numpy colour (H,W,4 uint8 BGRA) and depth (H,W float32) buffers per target."""
+    cols, deps = [], []
+    for (w, h) in handle.targets():
+        cols.append(np.zeros((h, w, 4), np.uint8))
+        deps.append(np.zeros((h, w), np.float32))
+    return cols, deps
+
+
+def pointer_arrays(cols, deps):
+    n = len(cols)
+    cp = (C.POINTER(C.c_uint8) * n)(*[c.ctypes.data_as(C.POINTER(C.c_uint8)) for c in cols])
+    dp = (C.POINTER(C.c_float) * n)(*[d.ctypes.data_as(C.POINTER(C.c_float)) for d in deps])
+    return cp, dp
