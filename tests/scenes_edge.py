@@ -1,0 +1,226 @@
+"""Hand-built edge-case scenes, shared by the fixture generator and the tests.
+
+Each builder takes a library that links the scene generator (product library,
+oracle or reference build) and returns a SceneHandle.  Positions are given in
+pixels and converted to clip space with w = 1 so ToWindow
+(rasterizer.cpp:239-253) lands on (or truncates to) the intended pixel.
+"""
+import struct
+
+import numpy as np
+
+from visor_gb300 import scene as vs
+
+
+def _color_vertex(px, py, z, rgba, w, h, clip_w=1.0):
+    x = (px / w * 2.0 - 1.0) * clip_w
+    y = (1.0 - py / h * 2.0) * clip_w
+    return struct.pack("<4f4B", x, y, z * clip_w, clip_w, *rgba)
+
+
+def _tri_scene(lib, w, h, tris, pipe_kw, clear=True, topology=vs.TOPOLOGY_TRIANGLE_LIST):
+    """tris: list of [(px, py, z, (r,g,b,a)), x3] drawn as one non-indexed draw."""
+    sh = vs.new_scene(lib)
+    s = sh.ptr
+    t = lib.vsc_add_target(s, w, h)
+    p = vs.make_pipeline(vs.SHADER_COLOR, topology=topology, **pipe_kw)
+    pi = lib.vsc_add_pipeline(s, p)
+    data = b"".join(_color_vertex(x, y, z, c, w, h) for tri in tris for (x, y, z, c) in tri)
+    off = lib.vsc_add_vertices(s, data, len(data))
+    nverts = len(data) // 20
+    d = vs.make_draw(pi, nverts, 0, indexed=False, vb_offset=off)
+    di = lib.vsc_add_draw(s, d)
+    lib.vsc_add_pass(s, t, 1 if clear else 0, di, 1)
+    return sh
+
+
+RED, GREEN, BLUE, HALF = (255, 0, 0, 255), (0, 255, 0, 255), (0, 0, 255, 255), (200, 100, 50, 128)
+
+
+def degenerate(lib):
+    # collinear, point, and a sliver that truncates to zero area
+    tris = [
+        [(4, 4, 0.5, RED), (20, 20, 0.5, RED), (36, 36, 0.5, RED)],
+        [(10, 30, 0.5, GREEN), (10, 30, 0.5, GREEN), (10, 30, 0.5, GREEN)],
+        [(40.2, 5, 0.5, BLUE), (40.7, 40, 0.5, BLUE), (40.4, 60, 0.5, BLUE)],
+        [(5, 50, 0.3, HALF), (30, 52, 0.3, HALF), (12, 62, 0.3, HALF)],
+    ]
+    return _tri_scene(lib, 64, 64, tris, {})
+
+
+def windings(lib, cull_mode, front_face):
+    ccw = [(4, 30, 0.5, RED), (28, 30, 0.5, RED), (16, 4, 0.5, RED)]
+    cw = [(36, 4, 0.5, GREEN), (60, 30, 0.5, GREEN), (36, 30, 0.5, GREEN)]
+    return _tri_scene(lib, 64, 40, [ccw, cw], {"cull_mode": cull_mode, "front_face": front_face})
+
+
+def depth_ops(lib, op, write=1, depth_test=1):
+    # two coplanar overlapping triangles (ties), then one nearer and one farther
+    a = [(4, 4, 0.5, RED), (56, 8, 0.5, RED), (10, 56, 0.5, RED)]
+    b = [(8, 10, 0.5, GREEN), (60, 20, 0.5, GREEN), (30, 60, 0.5, GREEN)]
+    c = [(0, 30, 0.25, BLUE), (64, 28, 0.75, BLUE), (32, 63, 0.1, BLUE)]
+    d = [(20, 0, 0.9, HALF), (63, 40, 0.9, HALF), (40, 63, 0.2, HALF)]
+    return _tri_scene(lib, 64, 64, [a, b, c, d],
+                      {"depth_op": op, "depth_write": write, "depth_test": depth_test})
+
+
+def blend_overlap(lib, seed=5, n=60):
+    rng = np.random.default_rng(seed)
+    tris = []
+    for _ in range(n):
+        cx, cy = rng.uniform(-8, 72, 2)
+        pts = []
+        for k in range(3):
+            pts.append((float(cx + rng.uniform(-20, 20)), float(cy + rng.uniform(-20, 20)),
+                        float(rng.uniform(0, 1)),
+                        (int(rng.integers(0, 256)), int(rng.integers(0, 256)),
+                         int(rng.integers(0, 256)), int(rng.integers(40, 256)))))
+        tris.append(pts)
+    return _tri_scene(lib, 64, 64, tris, {"depth_op": vs.CMP_LEQUAL, "blend_enable": 1,
+                                          "src_factor": vs.BLEND_SRC_ALPHA,
+                                          "dst_factor": vs.BLEND_ONE_MINUS_SRC_ALPHA})
+
+
+def shared_edges(lib):
+    # a quad split along its diagonal, blended: the shared edge is drawn twice (no top-left rule)
+    q = [(8, 8, 0.5, HALF), (56, 8, 0.5, HALF), (56, 56, 0.5, HALF), (8, 56, 0.5, HALF)]
+    tris = [[q[0], q[1], q[2]], [q[0], q[2], q[3]]]
+    return _tri_scene(lib, 64, 64, tris, {"depth_test": 0, "blend_enable": 1,
+                                          "src_factor": vs.BLEND_SRC_ALPHA,
+                                          "dst_factor": vs.BLEND_ONE_MINUS_SRC_ALPHA})
+
+
+def offscreen(lib):
+    # partly off every edge, fully off-screen, and touching the never-drawn last row/column
+    tris = [
+        [(-30, -20, 0.5, RED), (40, 10, 0.5, RED), (5, 50, 0.5, RED)],
+        [(50, 30, 0.4, GREEN), (100, 40, 0.4, GREEN), (60, 90, 0.4, GREEN)],
+        [(-50, -50, 0.3, BLUE), (-10, -40, 0.3, BLUE), (-30, -5, 0.3, BLUE)],
+        [(0, 0, 0.2, HALF), (64, 0, 0.2, HALF), (64, 64, 0.2, HALF)],
+    ]
+    return _tri_scene(lib, 64, 64, tris, {})
+
+
+def strip(lib):
+    verts = []
+    for i in range(12):
+        x = 4 + i * 5
+        y = 10 if i % 2 == 0 else 50
+        verts.append((x, y, 0.1 + 0.05 * i, (i * 20 % 256, 255 - i * 20 % 256, 128, 255)))
+    return _tri_scene(lib, 64, 64, [verts[i:i + 1] for i in range(12)], {},
+                      topology=vs.TOPOLOGY_TRIANGLE_STRIP)
+
+
+def load_pass(lib):
+    """Two passes on one target: the second loads (no clear) and blends over the first."""
+    sh = vs.new_scene(lib)
+    s = sh.ptr
+    w = h = 48
+    t = lib.vsc_add_target(s, w, h)
+    p1 = lib.vsc_add_pipeline(s, vs.make_pipeline(vs.SHADER_COLOR))
+    p2 = lib.vsc_add_pipeline(s, vs.make_pipeline(
+        vs.SHADER_COLOR, depth_op=vs.CMP_ALWAYS, blend_enable=1, src_factor=vs.BLEND_SRC_ALPHA,
+        dst_factor=vs.BLEND_ONE_MINUS_SRC_ALPHA))
+    a = [(2, 2, 0.5, RED), (46, 4, 0.5, RED), (4, 46, 0.5, RED)]
+    b = [(46, 46, 0.7, HALF), (2, 40, 0.7, HALF), (40, 2, 0.7, HALF)]
+    da = b"".join(_color_vertex(x, y, z, c, w, h) for (x, y, z, c) in a)
+    db = b"".join(_color_vertex(x, y, z, c, w, h) for (x, y, z, c) in b)
+    oa = lib.vsc_add_vertices(s, da, len(da))
+    ob = lib.vsc_add_vertices(s, db, len(db))
+    d1 = lib.vsc_add_draw(s, vs.make_draw(p1, 3, 0, vb_offset=oa))
+    d2 = lib.vsc_add_draw(s, vs.make_draw(p2, 3, 0, vb_offset=ob))
+    lib.vsc_add_pass(s, t, 1, d1, 1)
+    lib.vsc_add_pass(s, t, 0, d2, 1)
+    return sh
+
+
+def texture_wrap(lib):
+    """Lambert-textured quads whose uv run negative and past 1 (repeat addressing)."""
+    sh = vs.new_scene(lib)
+    s = sh.ptr
+    w = h = 64
+    t = lib.vsc_add_target(s, w, h)
+    pi = lib.vsc_add_pipeline(s, vs.make_pipeline(vs.SHADER_LAMBERT_TEX))
+    tex = lib.vsc_add_texture(s, 8, 8, 1, None, 99)
+    verts = []
+    quads = [((-0.9, -0.9), (0.0, 0.0), (-0.3, -0.2), (0.45, 0.55)),
+             ((0.05, 0.05), (0.9, 0.9), (0.0, 0.0), (1.0, 1.0)),
+             ((-0.9, 0.05), (-0.05, 0.9), (0.75, 0.2), (2.25, 3.7))]
+    idx = []
+    for (x0, y0), (x1, y1), (u0, v0), (u1, v1) in quads:
+        base = len(verts)
+        for (x, y, u, v) in ((x0, y0, u0, v0), (x1, y0, u1, v0), (x1, y1, u1, v1), (x0, y1, u0, v1)):
+            verts.append(struct.pack("<8f", x, y, 0.5, 0.0, 0.3, 1.0, u, v))
+        idx += [base, base + 1, base + 2, base, base + 2, base + 3]
+    data = b"".join(verts)
+    off = lib.vsc_add_vertices(s, data, len(data))
+    ia = np.array(idx, np.uint32)
+    first = lib.vsc_add_indices(s, ia.ctypes.data, len(ia))
+    ident = struct.pack("<16f", 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1)
+    light = struct.pack("<4f", 0.0, 0.6, 0.8, 0.0)
+    d = vs.make_draw(pi, len(idx), int(first), indexed=True, texture=tex, vb_offset=off,
+                     push=ident + light)
+    di = lib.vsc_add_draw(s, d)
+    lib.vsc_add_pass(s, t, 1, di, 1)
+    return sh
+
+
+EDGE_SCENES = {
+    "degenerate": degenerate,
+    "winding_none_ccw": lambda lib: windings(lib, vs.CULL_NONE, vs.FRONT_CCW),
+    "winding_back_ccw": lambda lib: windings(lib, vs.CULL_BACK, vs.FRONT_CCW),
+    "winding_front_ccw": lambda lib: windings(lib, vs.CULL_FRONT, vs.FRONT_CCW),
+    "winding_back_cw": lambda lib: windings(lib, vs.CULL_BACK, vs.FRONT_CW),
+    "winding_both_cw": lambda lib: windings(lib, vs.CULL_FRONT_AND_BACK, vs.FRONT_CW),
+    "depth_less": lambda lib: depth_ops(lib, vs.CMP_LESS),
+    "depth_lequal": lambda lib: depth_ops(lib, vs.CMP_LEQUAL),
+    "depth_equal": lambda lib: depth_ops(lib, vs.CMP_EQUAL),
+    "depth_greater": lambda lib: depth_ops(lib, vs.CMP_GREATER),
+    "depth_gequal": lambda lib: depth_ops(lib, vs.CMP_GEQUAL),
+    "depth_not_equal": lambda lib: depth_ops(lib, vs.CMP_NOT_EQUAL),
+    "depth_never": lambda lib: depth_ops(lib, vs.CMP_NEVER),
+    "depth_always": lambda lib: depth_ops(lib, vs.CMP_ALWAYS),
+    "depth_less_nowrite": lambda lib: depth_ops(lib, vs.CMP_LESS, write=0),
+    "depth_disabled": lambda lib: depth_ops(lib, vs.CMP_LESS, depth_test=0),
+    "blend_overlap": blend_overlap,
+    "shared_edges": shared_edges,
+    "offscreen": offscreen,
+    "strip": strip,
+    "load_pass": load_pass,
+    "texture_wrap": texture_wrap,
+}
+
+# Generated configurations pinned by fixtures: name -> (config, seed, params)
+CONFIG_SCENES = {
+    "cfg1_sphere": (1, 7, {}),
+    "cfg1_sphere_cull_cw": (1, 11, {"flags": vs.FLAG_BACKFACE_CULL | vs.FLAG_CLOCKWISE}),
+    "cfg1_frames4": (1, 21, {"count": 4, "width": 128, "height": 128}),
+    "cfg2_small_blend": (2, 3, {"width": 256, "height": 192, "count": 3000, "max_area": 2000.0}),
+    "cfg2_small_opaque": (2, 4, {"width": 256, "height": 192, "count": 2000, "max_area": 2000.0,
+                                 "flags": vs.FLAG_NO_BLEND}),
+    "cfg2_medium_blend": (2, 17, {"width": 640, "height": 360, "count": 40000}),
+    "cfg3_small_bilinear": (3, 9, {"width": 320, "height": 200, "count": 40, "max_tris": 3000,
+                                   "flags": vs.FLAG_FILTER_REFERENCE, "textures": 4,
+                                   "tex_size": 64}),
+    "cfg4_small": (4, 5, {"count": 6, "min_tris": 200, "max_tris": 3000}),
+    "cfg5_request_bilinear": (5, 13, {"count": 2, "max_tris": 20000, "textures": 4,
+                                      "tex_size": 128, "flags": vs.FLAG_FILTER_REFERENCE}),
+}
+
+# Scenes whose parity is this project's specification (no reference implementation).
+SPEC_SCENES = {
+    "cfg3_small_trilinear": (3, 9, {"width": 320, "height": 200, "count": 40, "max_tris": 3000,
+                                    "textures": 4, "tex_size": 64}),
+    "cfg5_request_trilinear": (5, 13, {"count": 2, "max_tris": 20000, "textures": 4,
+                                       "tex_size": 128}),
+}
+
+
+def build(lib, name):
+    if name in EDGE_SCENES:
+        return EDGE_SCENES[name](lib)
+    cfg, seed, params = CONFIG_SCENES.get(name) or SPEC_SCENES[name]
+    return vs.generate(lib, cfg, seed, **params)
+
+
+ALL_PINNED = list(EDGE_SCENES) + list(CONFIG_SCENES)
