@@ -20,6 +20,10 @@
 extern "C" {
 #endif
 
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 typedef void (*vsd_void_fn)(void);
 typedef vsd_void_fn (*vsd_get_proc_fn)(void *instance, const char *name);
 
@@ -55,8 +59,15 @@ int vsd_read_target(vsd_scene *s, uint32_t target, uint8_t *color, float *depth)
 
 void vsd_release(vsd_scene *s);
 
+/* The VkQueue the context submits to. */
+void *vsd_queue(vsd_context *ctx);
+
 /* Bytes copied host->device per submit when VSD_RESTAGE_INPUTS is set. */
 uint64_t vsd_restage_bytes(const vsd_scene *s);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #ifdef __cplusplus
 }

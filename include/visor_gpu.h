@@ -1,0 +1,132 @@
+/*
+ * visor_gpu.h - the thin C ABI between the Vulkan ICD front end (C++) and the
+ * CUDA back end of the draw path.  Plain pointers and sizes only.
+ *
+ * It replaces the reference's direct C++ calls from command replay into the
+ * CPU rasterizer: vkQueueSubmit (cmd_exec.cpp:187-201) lowers a recorded
+ * command buffer into a vgpu command list (copies, render-pass clears, draw
+ * jobs) and hands it to vgpu_submit; vkCreateGraphicsPipelines
+ * (shaders.cpp:27-91) hands the translated shaders to vgpu_program_create;
+ * vkAllocateMemory (memory.cpp:3-13) becomes vgpu_mem_alloc.  Every function
+ * returns 0 on success or a negative VkResult-compatible code.
+ */
+#ifndef VISOR_GPU_H
+#define VISOR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../visor_gb300/csrc/kernels/vgx_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* VkResult codes returned through this ABI */
+#define VGPU_OK 0
+#define VGPU_TIMEOUT 2
+#define VGPU_ERROR_OUT_OF_HOST_MEMORY (-1)
+#define VGPU_ERROR_OUT_OF_DEVICE_MEMORY (-2)
+#define VGPU_ERROR_INITIALIZATION_FAILED (-3)
+#define VGPU_ERROR_DEVICE_LOST (-4)
+
+typedef struct vgpu_program vgpu_program;
+typedef struct vgpu_queue vgpu_queue;
+typedef struct vgpu_fence vgpu_fence;
+typedef struct vgpu_list vgpu_list;
+
+typedef struct vgpu_device_info {
+  char name[256];
+  uint64_t total_memory;
+  uint32_t sm_count;
+  uint32_t cc_major, cc_minor;
+} vgpu_device_info;
+
+int vgpu_init(void);
+int vgpu_device_info_get(vgpu_device_info *out);
+
+/* Device memory (device_ptr) with an optional pinned host mirror (host_ptr). */
+int vgpu_mem_alloc(uint64_t bytes, int host_visible, void **device_ptr, void **host_ptr);
+void vgpu_mem_free(void *device_ptr, void *host_ptr);
+
+/*
+ * Compile the stage kernels for one shader pair.  `shader_source` is CUDA C++
+ * produced by the SPIR-V translator; it defines VGX_K, VGX_LOD_SLOT,
+ * VGX_LOD_TEX, vgx_vs and vgx_fs.  NVRTC compiles it for sm_103a with the
+ * fixed-function stage kernels.  Compiled images are cached by source hash.
+ */
+int vgpu_program_create(const char *shader_source, uint32_t tile_shift, vgpu_program **out,
+                        char *log, size_t log_size);
+void vgpu_program_destroy(vgpu_program *p);
+/* NVRTC-compile only (no device needed); cubin_bytes receives the image size. */
+int vgpu_program_check(const char *shader_source, uint32_t tile_shift, char *log, size_t log_size,
+                       uint64_t *cubin_bytes);
+uint32_t vgpu_program_record_words(const vgpu_program *p);
+
+/* Command lists: built once per recorded command buffer, replayed per submit. */
+vgpu_list *vgpu_list_create(void);
+void vgpu_list_destroy(vgpu_list *l);
+/* device-to-device copy (vkCmdCopyBuffer / vkCmdCopyBufferToImage) */
+void vgpu_list_copy(vgpu_list *l, void *dst, const void *src, uint64_t bytes);
+/* clear a target's colour and/or depth (BeginRenderPass with loadOp CLEAR) */
+void vgpu_list_clear(vgpu_list *l, const VgxTarget *target, int color, int depth);
+/* one draw; consecutive draws with the same program may be merged into one job */
+void vgpu_list_draw(vgpu_list *l, vgpu_program *prog, const VgxDraw *draw, const VgxTarget *target);
+/* host-visible memory refresh before (upload) and after (download) the list */
+void vgpu_list_upload(vgpu_list *l, void *dev, const void *host, uint64_t bytes);
+void vgpu_list_download(vgpu_list *l, void *host, const void *dev, uint64_t bytes);
+
+/* Execution modes of a list (set before the first submit). */
+enum {
+  VGPU_MODE_BATCHED = 0, /* merge draws into jobs, fuse clears into the raster, CUDA-graph replay */
+  VGPU_MODE_PER_DRAW = 1 /* one job and one set of launches per draw, separate clears */
+};
+void vgpu_list_set_mode(vgpu_list *l, int mode);
+
+int vgpu_queue_create(vgpu_queue **out);
+void vgpu_queue_destroy(vgpu_queue *q);
+/* Enqueue a list; returns once work is queued (and, when pair storage must grow, after one sync). */
+int vgpu_submit(vgpu_queue *q, vgpu_list *l);
+int vgpu_fence_create(vgpu_fence **out);
+int vgpu_fence_signal(vgpu_queue *q, vgpu_fence *f);
+/* Wait up to timeout_ns; returns VGPU_OK, VGPU_TIMEOUT or an error. */
+int vgpu_fence_wait(vgpu_fence *f, uint64_t timeout_ns);
+int vgpu_fence_status(vgpu_fence *f);
+void vgpu_fence_reset(vgpu_fence *f);
+void vgpu_fence_destroy(vgpu_fence *f);
+int vgpu_queue_wait_idle(vgpu_queue *q);
+
+/* Statistics since the queue was created or last reset (synchronises the queue). */
+typedef struct vgpu_stats {
+  uint64_t tris_in, tris_out, tested, covered, shaded, draws, jobs, pairs;
+  uint64_t kernel_launches;
+  double gpu_ms;       /* device time of the last submit (CUDA events on the queue's stream) */
+  double raster_ms;    /* device time spent in raster kernels of the last submit */
+  uint32_t status;     /* sticky device status bits */
+} vgpu_stats;
+int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out);
+void vgpu_queue_reset_stats(vgpu_queue *q);
+/* Stream the queue launches on (cudaStream_t), for callers that time around it. */
+void *vgpu_queue_stream(vgpu_queue *q);
+
+/* Tuning knobs read at list build time (autotuner, see tune.py). */
+typedef struct vgpu_tuning {
+  uint32_t raster_blocks_per_sm; /* persistent raster CTAs per SM */
+  uint32_t use_graphs;           /* replay batched lists as CUDA graphs */
+} vgpu_tuning;
+void vgpu_set_tuning(const vgpu_tuning *t);
+void vgpu_get_tuning(vgpu_tuning *t);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,60 @@
+/*
+ * visor_icd.h - the drop-in boundary: what libvisor_gb300.so exports.
+ *
+ * The library is a Vulkan installable client driver, like the reference
+ * (visor.json names the library; the Vulkan loader dlopens it).  The loader
+ * binds exactly these three C symbols and reaches every vk* entry point
+ * through them:
+ *
+ *   vk_icdNegotiateLoaderICDInterfaceVersion  replaces icd_interface.cpp:161-169
+ *   vk_icdGetInstanceProcAddr                 replaces icd_interface.cpp:132-148
+ *   vk_icdGetPhysicalDeviceProcAddr           replaces icd_interface.cpp:150-159
+ *
+ * vkGetDeviceProcAddr (icd_interface.cpp:115-123) is returned through them.
+ * The vk* set is the reference's CHECK_INST_FUNCS / CHECK_PHYS_FUNCS /
+ * CHECK_DEV_FUNCS tables (icd_interface.cpp:7-102) minus the Win32 WSI
+ * entries; unknown names return NULL (the reference returns a strdup'd string
+ * that crashes when called).  The vk* functions are also exported under their
+ * standard names, with the Vulkan 1.0 signatures of include/visor_vk.h.
+ *
+ * Besides the Vulkan surface the library exports a few visor_gb300_* calls
+ * that have no counterpart in the reference: execution mode and statistics
+ * for benchmarks and tests.
+ */
+#ifndef VISOR_ICD_H
+#define VISOR_ICD_H
+
+#include "visor_gpu.h"
+#include "visor_vk.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+VkResult vk_icdNegotiateLoaderICDInterfaceVersion(uint32_t *pSupportedVersion);
+PFN_vkVoidFunction vk_icdGetInstanceProcAddr(VkInstance instance, const char *pName);
+PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, const char *pName);
+PFN_vkVoidFunction vkGetDeviceProcAddr(VkDevice device, const char *pName);
+
+/* Execution mode for command buffers lowered after this call: VGPU_MODE_BATCHED
+   (default) or VGPU_MODE_PER_DRAW.  The environment variable VISOR_GB300_MODE
+   ("batched" / "per_draw") sets the initial value. */
+void visor_gb300_set_mode(int mode);
+int visor_gb300_get_mode(void);
+
+/* Queue statistics (rasterizer counters, launches, device time of the last submit). */
+int visor_gb300_queue_stats(VkQueue queue, vgpu_stats *out);
+void visor_gb300_queue_reset_stats(VkQueue queue);
+
+/* SPIR-V pair -> CUDA source, without a device (returns 0 and err on failure). */
+size_t visor_gb300_translate(const uint32_t *vs_words, size_t vs_count, const uint32_t *fs_words,
+                             size_t fs_count, char *out, size_t size, char *err, size_t err_size);
+
+/* Translated CUDA source of a pipeline (for inspection and tests); returns bytes written. */
+size_t visor_gb300_pipeline_source(VkPipeline pipeline, char *buf, size_t size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

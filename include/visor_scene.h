@@ -24,6 +24,10 @@
 extern "C" {
 #endif
 
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 /* Shader pairs the generator can emit (as SPIR-V through visor_spirv_emit). */
 enum {
   VSC_SHADER_LAMBERT_TEX = 1,       /* pos/normal/uv; MVP push constant; tex * max(dot(N,L),0) */
@@ -190,6 +194,10 @@ double vsc_sin(double x);
 double vsc_cos(double x);
 double vsc_exp(double x);
 double vsc_log(double x);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #ifdef __cplusplus
 }

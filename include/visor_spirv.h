@@ -18,6 +18,10 @@
 extern "C" {
 #endif
 
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 enum { VSPV_STAGE_VERTEX = 0, VSPV_STAGE_FRAGMENT = 4 };
 
 /*
@@ -26,6 +30,10 @@ enum { VSPV_STAGE_VERTEX = 0, VSPV_STAGE_FRAGMENT = 4 };
  * too small, so callers can size the buffer), or 0 for an unknown shader.
  */
 size_t vspv_emit(uint32_t shader, uint32_t stage, uint32_t *words, size_t capacity);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #ifdef __cplusplus
 }

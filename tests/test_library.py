@@ -1,0 +1,57 @@
+"""The C-ABI library without a GPU: it loads, exports every declared entry
+point, negotiates the loader interface, answers proc-address queries, and its
+SPIR-V translator output compiles with NVRTC for sm_103a."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import visor_gb300 as vg
+from conftest import REPO
+from visor_gb300 import scene as vs
+
+HEADERS = ["visor_icd.h", "visor_gpu.h", "visor_driver.h", "visor_scene.h", "visor_spirv.h"]
+
+
+def _declared(header):
+    text = open(os.path.join(REPO, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = "\n".join(l for l in text.splitlines() if not l.lstrip().startswith("typedef"))
+    names = re.findall(r"^[A-Za-z_][\w \*]*?\b((?:vk|vgpu|vsd|vsc|vspv|visor_gb300)\w*)\s*\(", text, re.M)
+    return sorted(set(n for n in names if not n.startswith("PFN")))
+
+
+@pytest.mark.parametrize("header", HEADERS)
+def test_exports_every_declared_symbol(header):
+    lib = C.CDLL(vg.LIB_PATH)
+    names = _declared(header)
+    assert names, header
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_loader_negotiation_and_proc_addr():
+    L = vg.lib()
+    v = C.c_uint32(7)
+    assert L.vk_icdNegotiateLoaderICDInterfaceVersion(C.byref(v)) == 0
+    assert v.value == 4
+    v = C.c_uint32(2)
+    assert L.vk_icdNegotiateLoaderICDInterfaceVersion(C.byref(v)) == 0 and v.value == 2
+    assert L.vk_icdNegotiateLoaderICDInterfaceVersion(None) != 0
+    for name in [b"vkCreateInstance", b"vkQueueSubmit", b"vkCmdDrawIndexed", b"vkCreateGraphicsPipelines",
+                 b"vkGetDeviceProcAddr", b"vkGetPhysicalDeviceMemoryProperties"]:
+        assert L.vk_icdGetInstanceProcAddr(None, name)
+    assert not L.vk_icdGetInstanceProcAddr(None, b"vkNotAFunction")
+
+
+@pytest.mark.parametrize("shader", [vs.SHADER_LAMBERT_TEX, vs.SHADER_COLOR, vs.SHADER_LAMBERT_TEX_ALPHA])
+def test_translated_shaders_compile_for_sm103a(shader):
+    src = vg.translate(vg.spirv(shader, 0), vg.spirv(shader, 4))
+    assert "vgx_vs" in src and "vgx_fs" in src
+    assert vg.nvrtc_check(src) > 10000
+
+
+def test_translator_rejects_garbage():
+    with pytest.raises(ValueError):
+        vg.translate([1, 2, 3, 4, 5, 6], vg.spirv(vs.SHADER_COLOR, 4))

@@ -1,1 +1,237 @@
-"""GB300-native draw path for the Visor Vulkan ICD."""
+"""GB300-native draw path for the Visor Vulkan ICD.
+
+libvisor_gb300.so (built in-tree by visor_gb300/build.py) is a Vulkan
+installable client driver: the loader-facing C ABI of include/visor_icd.h,
+a SPIR-V -> CUDA translator compiled with NVRTC for sm_103a at pipeline
+creation, and hand-written CUDA stage kernels.  This module loads the library
+and mirrors the path the reference's users take (record a command buffer,
+vkQueueSubmit, map the render targets) through the same scene driver the
+tests and benchmarks use.  It never falls back to a CPU path: if the library
+or a GPU is missing, calls fail loudly.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import scene as vscene
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libvisor_gb300.so")
+
+MODE_BATCHED = 0
+MODE_PER_DRAW = 1
+
+RESTAGE_INPUTS = 1
+DEVICE_TARGETS = 2
+
+_lib = None
+
+
+class VgpuStats(C.Structure):
+    _fields_ = [("tris_in", C.c_uint64), ("tris_out", C.c_uint64), ("tested", C.c_uint64),
+                ("covered", C.c_uint64), ("shaded", C.c_uint64), ("draws", C.c_uint64),
+                ("jobs", C.c_uint64), ("pairs", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("gpu_ms", C.c_double), ("raster_ms", C.c_double), ("status", C.c_uint32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class VgpuTuning(C.Structure):
+    _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("use_graphs", C.c_uint32)]
+
+
+def lib():
+    """Load (once) the in-tree library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run `python -m visor_gb300.build` first")
+    L = vscene.bind_scene_api(C.CDLL(LIB_PATH))
+    VP = C.c_void_p
+    L.vk_icdGetInstanceProcAddr.argtypes = [VP, C.c_char_p]
+    L.vk_icdGetInstanceProcAddr.restype = VP
+    L.vk_icdNegotiateLoaderICDInterfaceVersion.argtypes = [C.POINTER(C.c_uint32)]
+    L.vk_icdNegotiateLoaderICDInterfaceVersion.restype = C.c_int
+    L.vsd_create.argtypes = [VP, VP, C.POINTER(VP)]
+    L.vsd_create.restype = C.c_int
+    L.vsd_destroy.argtypes = [VP]
+    L.vsd_upload.argtypes = [VP, C.POINTER(vscene.Scene), C.c_uint32, C.POINTER(VP)]
+    L.vsd_upload.restype = C.c_int
+    L.vsd_submit.argtypes = [VP]
+    L.vsd_submit.restype = C.c_int
+    L.vsd_submit_async.argtypes = [VP]
+    L.vsd_submit_async.restype = C.c_int
+    L.vsd_wait.argtypes = [VP, C.c_uint64]
+    L.vsd_wait.restype = C.c_int
+    L.vsd_read_target.argtypes = [VP, C.c_uint32, VP, VP]
+    L.vsd_read_target.restype = C.c_int
+    L.vsd_release.argtypes = [VP]
+    L.vsd_queue.argtypes = [VP]
+    L.vsd_queue.restype = VP
+    L.vsd_restage_bytes.argtypes = [VP]
+    L.vsd_restage_bytes.restype = C.c_uint64
+    L.vspv_emit.argtypes = [C.c_uint32, C.c_uint32, VP, C.c_size_t]
+    L.vspv_emit.restype = C.c_size_t
+    L.visor_gb300_set_mode.argtypes = [C.c_int]
+    L.visor_gb300_get_mode.restype = C.c_int
+    L.visor_gb300_queue_stats.argtypes = [VP, C.POINTER(VgpuStats)]
+    L.visor_gb300_queue_stats.restype = C.c_int
+    L.visor_gb300_queue_reset_stats.argtypes = [VP]
+    L.visor_gb300_translate.argtypes = [VP, C.c_size_t, VP, C.c_size_t, C.c_char_p, C.c_size_t,
+                                        C.c_char_p, C.c_size_t]
+    L.visor_gb300_translate.restype = C.c_size_t
+    L.vgpu_program_check.argtypes = [C.c_char_p, C.c_uint32, C.c_char_p, C.c_size_t,
+                                     C.POINTER(C.c_uint64)]
+    L.vgpu_program_check.restype = C.c_int
+    L.vgpu_set_tuning.argtypes = [C.POINTER(VgpuTuning)]
+    L.vgpu_get_tuning.argtypes = [C.POINTER(VgpuTuning)]
+    _lib = L
+    return L
+
+
+def spirv(shader, stage):
+    """SPIR-V words (numpy uint32) of one stage (0 vertex, 4 fragment) of a scene shader pair."""
+    L = lib()
+    n = L.vspv_emit(shader, stage, None, 0)
+    buf = np.zeros(n, np.uint32)
+    L.vspv_emit(shader, stage, buf.ctypes.data, n)
+    return buf
+
+
+def translate(vs_words, fs_words):
+    """CUDA source the pipeline compiler produces for a SPIR-V pair (no GPU needed)."""
+    L = lib()
+    vs = np.ascontiguousarray(vs_words, np.uint32)
+    fs = np.ascontiguousarray(fs_words, np.uint32)
+    err = C.create_string_buffer(4096)
+    n = L.visor_gb300_translate(vs.ctypes.data, len(vs), fs.ctypes.data, len(fs), None, 0, err, 4096)
+    if n == 0:
+        raise ValueError("translation failed: " + err.value.decode())
+    out = C.create_string_buffer(n + 1)
+    L.visor_gb300_translate(vs.ctypes.data, len(vs), fs.ctypes.data, len(fs), out, n + 1, err, 4096)
+    return out.value.decode()
+
+
+def nvrtc_check(source, tile_shift=3):
+    """NVRTC-compile translated source with the stage kernels for sm_103a; returns cubin bytes."""
+    L = lib()
+    log = C.create_string_buffer(65536)
+    nbytes = C.c_uint64(0)
+    rc = L.vgpu_program_check(source.encode(), tile_shift, log, 65536, C.byref(nbytes))
+    if rc != 0:
+        raise RuntimeError("NVRTC failed:\n" + log.value.decode())
+    return int(nbytes.value)
+
+
+def set_mode(mode):
+    lib().visor_gb300_set_mode(mode)
+
+
+def set_tuning(raster_blocks_per_sm=None, use_graphs=None):
+    L = lib()
+    t = VgpuTuning()
+    L.vgpu_get_tuning(C.byref(t))
+    if raster_blocks_per_sm is not None:
+        t.raster_blocks_per_sm = raster_blocks_per_sm
+    if use_graphs is not None:
+        t.use_graphs = use_graphs
+    L.vgpu_set_tuning(C.byref(t))
+
+
+class Device:
+    """An ICD instance/device/queue created through vk_icdGetInstanceProcAddr."""
+
+    def __init__(self):
+        L = lib()
+        self.lib = L
+        ctx = C.c_void_p()
+        gpa = C.cast(L.vk_icdGetInstanceProcAddr, C.c_void_p)
+        rc = L.vsd_create(gpa, None, C.byref(ctx))
+        if rc != 0:
+            raise RuntimeError(f"ICD device creation failed (VkResult {rc}); a CUDA GPU is required")
+        self.ctx = ctx
+
+    @property
+    def queue(self):
+        return self.lib.vsd_queue(self.ctx)
+
+    def stats(self):
+        s = VgpuStats()
+        rc = self.lib.visor_gb300_queue_stats(self.queue, C.byref(s))
+        if rc != 0:
+            raise RuntimeError(f"queue stats failed: {rc}")
+        return s.as_dict()
+
+    def reset_stats(self):
+        self.lib.visor_gb300_queue_reset_stats(self.queue)
+
+    def upload(self, handle, flags=0):
+        """Create every Vulkan object of a scene and record its command buffer."""
+        sc = C.c_void_p()
+        rc = self.lib.vsd_upload(self.ctx, handle.ptr, flags, C.byref(sc))
+        if rc != 0:
+            raise RuntimeError(f"scene upload failed (VkResult {rc})")
+        return UploadedScene(self, handle, sc)
+
+    def close(self):
+        if self.ctx:
+            self.lib.vsd_destroy(self.ctx)
+            self.ctx = None
+
+
+class UploadedScene:
+    def __init__(self, dev, handle, sc):
+        self.dev = dev
+        self.handle = handle
+        self.sc = sc
+
+    def submit(self):
+        rc = self.dev.lib.vsd_submit(self.sc)
+        if rc != 0:
+            raise RuntimeError(f"vkQueueSubmit/vkWaitForFences failed (VkResult {rc})")
+
+    def submit_async(self):
+        rc = self.dev.lib.vsd_submit_async(self.sc)
+        if rc != 0:
+            raise RuntimeError(f"vkQueueSubmit failed (VkResult {rc})")
+
+    def wait(self, timeout_ns=2 ** 64 - 1):
+        return self.dev.lib.vsd_wait(self.sc, timeout_ns)
+
+    def read(self):
+        cols, deps = vscene.target_buffers(self.handle)
+        for i, (c, d) in enumerate(zip(cols, deps)):
+            rc = self.dev.lib.vsd_read_target(self.sc, i, c.ctypes.data, d.ctypes.data)
+            if rc != 0:
+                raise RuntimeError(f"reading target {i} failed ({rc})")
+        return cols, deps
+
+    def restage_bytes(self):
+        return int(self.dev.lib.vsd_restage_bytes(self.sc))
+
+    def release(self):
+        if self.sc:
+            self.dev.lib.vsd_release(self.sc)
+            self.sc = None
+
+
+def render(handle, mode=MODE_BATCHED, device=None):
+    """Render a scene through the ICD; returns (colours, depths, counters)."""
+    own = device is None
+    dev = device or Device()
+    set_mode(mode)
+    dev.reset_stats()
+    up = dev.upload(handle)
+    try:
+        up.submit()
+        cols, deps = up.read()
+        st = dev.stats()
+    finally:
+        up.release()
+        if own:
+            dev.close()
+    counters = {k: int(st[k]) for k in ("tris_in", "tris_out", "tested", "covered", "shaded", "draws")}
+    return cols, deps, counters

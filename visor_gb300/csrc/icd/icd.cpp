@@ -1,0 +1,1668 @@
+/*
+ * icd.cpp - the Vulkan ICD front end of the GB300 draw path.
+ *
+ * Same object model and entry points as the reference ICD
+ * (icd_stubs.cpp, query.cpp, memory.cpp, buffers.cpp, images.cpp,
+ * descriptors.cpp, renderpass.cpp, shaders.cpp, cmd_alloc.cpp, cmd_record.cpp,
+ * cmd_exec.cpp, icd_interface.cpp), with the storage and the replay moved to
+ * the GPU:
+ *   - VkDeviceMemory is a device allocation; host-visible memory also has a
+ *     pinned host copy that vkMapMemory returns and that each submission
+ *     uploads (before) and downloads (after) when the command buffer reads or
+ *     writes it;
+ *   - vkCreateShaderModule parses SPIR-V; vkCreateGraphicsPipelines translates
+ *     the stage pair to CUDA C++ and compiles it with NVRTC for sm_103a;
+ *   - vkCmd* append packets to a command stream (as cmd_record.cpp does);
+ *     the stream is lowered once into a vgpu command list and vkQueueSubmit
+ *     replays that list on a CUDA stream; fences are CUDA events.
+ * Replay keeps the reference's state rules (cmd_exec.cpp:15-185): colour
+ * attachment 0 and the depth attachment of subpass 0, clear values consumed
+ * in order, depth kept across EndRenderPass, vertexOffset/instanceCount
+ * ignored, viewport and scissor recorded but not applied.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "visor_icd.h"
+#include "../spirv/translate.h"
+
+#define VISOR_EXPORT extern "C" __attribute__((visibility("default")))
+
+/* ------------------------------------------------------------------------ */
+/* objects                                                                   */
+/* ------------------------------------------------------------------------ */
+
+struct VkInstance_T
+{
+  uintptr_t loaderMagic;
+};
+
+struct VkPhysicalDevice_T
+{
+  uintptr_t loaderMagic;
+};
+
+struct VkQueue_T
+{
+  uintptr_t loaderMagic;
+  vgpu_queue *q = nullptr;
+};
+
+struct VkDevice_T
+{
+  uintptr_t loaderMagic;
+  VkQueue_T *queue = nullptr;
+  std::map<std::string, vgpu_program *> programs; /* by translated source */
+  std::mutex mu;
+};
+
+struct VkDeviceMemory_T
+{
+  VkDeviceSize size = 0;
+  uint32_t type = 0;
+  void *dptr = nullptr;
+  void *hptr = nullptr;
+};
+
+struct VkBuffer_T
+{
+  VkDeviceSize size = 0;
+  VkDeviceMemory_T *mem = nullptr;
+  VkDeviceSize offset = 0;
+};
+
+struct VkImage_T
+{
+  VkExtent3D extent = {0, 0, 0};
+  VkFormat format = VK_FORMAT_UNDEFINED;
+  uint32_t mips = 1, layers = 1, bpp = 4;
+  VkDeviceMemory_T *mem = nullptr;
+  VkDeviceSize offset = 0;
+};
+
+struct VkImageView_T
+{
+  VkImage_T *image = nullptr;
+  uint32_t base_mip = 0, levels = 1;
+};
+
+struct VkSampler_T
+{
+  uint32_t filter = VGX_FILTER_REFERENCE;
+};
+
+struct VkShaderModule_T
+{
+  vst::Module *mod = nullptr;
+};
+
+struct VkPipelineLayout_T
+{
+  int unused;
+};
+
+struct VkPipelineCache_T
+{
+  int unused;
+};
+
+struct VkDescriptorSetLayout_T
+{
+  uint32_t bindings = 0;
+};
+
+struct VkDescriptorPool_T
+{
+  int unused;
+};
+
+struct VkDescriptorSet_T
+{
+  struct Bind
+  {
+    VkDescriptorType type = VK_DESCRIPTOR_TYPE_MAX_ENUM;
+    VkImageView_T *view = nullptr;
+    VkSampler_T *sampler = nullptr;
+    VkBuffer_T *buffer = nullptr;
+    VkDeviceSize offset = 0, range = 0;
+  };
+  std::map<uint32_t, Bind> binds;
+};
+
+struct VkRenderPass_T
+{
+  int32_t color = -1, depth = -1;
+  bool color_clear = false, depth_clear = false;
+};
+
+struct VkFramebuffer_T
+{
+  std::vector<VkImageView_T *> views;
+};
+
+struct VkFence_T
+{
+  vgpu_fence *f = nullptr;
+  bool signaled = false;
+};
+
+struct VkSemaphore_T
+{
+  int unused;
+};
+
+struct VkPipeline_T
+{
+  struct Attr
+  {
+    uint32_t format = 0, binding = 0, offset = 0;
+  } attrs[VGX_MAX_ATTRS];
+  uint32_t strides[VGX_MAX_VB] = {0, 0, 0, 0};
+  uint32_t topology = 3, cull = 0, front = 0, depth_op = VK_COMPARE_OP_ALWAYS, depth_write = 0;
+  uint32_t blend = 0, src = 1, dst = 0, op = 0;
+  vgpu_program *prog = nullptr;
+  vst::Result tr;
+};
+
+struct VkCommandPool_T
+{
+  std::vector<VkCommandBuffer> buffers;
+};
+
+enum class Pkt : uint16_t
+{
+  BeginRP, EndRP, BindPipeline, BindSet, BindVB, BindIB, SetViewport, SetScissor, Push, Draw,
+  DrawIndexed, CopyBuf2Img, CopyBuf, Barrier
+};
+
+struct VkCommandBuffer_T
+{
+  uintptr_t loaderMagic;
+  VkCommandPool_T *pool = nullptr;
+  std::vector<uint8_t> stream;
+  vgpu_list *list = nullptr;
+  bool lowered = false;
+  int mode = -1;
+
+  template <typename T>
+  void push(Pkt k, const T &body)
+  {
+    size_t o = stream.size();
+    stream.resize(o + sizeof(uint16_t) + sizeof(T));
+    memcpy(&stream[o], &k, sizeof(uint16_t));
+    memcpy(&stream[o + sizeof(uint16_t)], &body, sizeof(T));
+  }
+  void push(Pkt k)
+  {
+    size_t o = stream.size();
+    stream.resize(o + sizeof(uint16_t));
+    memcpy(&stream[o], &k, sizeof(uint16_t));
+  }
+};
+
+namespace
+{
+int g_mode = -1;
+
+int default_mode()
+{
+  if(g_mode < 0)
+  {
+    const char *e = getenv("VISOR_GB300_MODE");
+    g_mode = (e && strcmp(e, "per_draw") == 0) ? VGPU_MODE_PER_DRAW : VGPU_MODE_BATCHED;
+  }
+  return g_mode;
+}
+
+template <typename T>
+T *mk()
+{
+  return new T();
+}
+
+void set_magic(void *p) { *(uintptr_t *)p = ICD_LOADER_MAGIC; }
+
+VkResult vr(int rc)
+{
+  switch(rc)
+  {
+    case VGPU_OK: return VK_SUCCESS;
+    case VGPU_TIMEOUT: return VK_TIMEOUT;
+    case VGPU_ERROR_OUT_OF_HOST_MEMORY: return VK_ERROR_OUT_OF_HOST_MEMORY;
+    case VGPU_ERROR_OUT_OF_DEVICE_MEMORY: return VK_ERROR_OUT_OF_DEVICE_MEMORY;
+    case VGPU_ERROR_INITIALIZATION_FAILED: return VK_ERROR_INITIALIZATION_FAILED;
+    default: return VK_ERROR_DEVICE_LOST;
+  }
+}
+
+uint32_t format_bpp(VkFormat f)
+{
+  /* images.cpp:20-36: 4 bytes per pixel except R8 and the BC formats (1) */
+  if(f == VK_FORMAT_R8_UNORM || f == VK_FORMAT_BC2_UNORM_BLOCK || f == VK_FORMAT_BC3_UNORM_BLOCK)
+    return 1;
+  return 4;
+}
+
+/* CalcSubresourceByteOffset (precompiled.cpp:3-36): tight mips, a layer holds every mip */
+VkDeviceSize subresource_offset(const VkImage_T *img, uint32_t mip, uint32_t layer)
+{
+  VkDeviceSize offs = 0;
+  const uint32_t w = img->extent.width, h = img->extent.height, bpp = img->bpp;
+  for(uint32_t m = 0; m < mip; m++)
+    offs += (VkDeviceSize)std::max(1u, w >> m) * std::max(1u, h >> m) * bpp;
+  if(layer > 0)
+  {
+    VkDeviceSize slice = 0;
+    for(uint32_t m = 0; m < img->mips; m++)
+      slice += (VkDeviceSize)std::max(1u, w >> m) * std::max(1u, h >> m) * bpp;
+    offs += slice * layer;
+  }
+  return offs;
+}
+
+uint8_t *dev_addr(VkDeviceMemory_T *m, VkDeviceSize off) { return m ? (uint8_t *)m->dptr + off : nullptr; }
+}    // namespace
+
+/* ------------------------------------------------------------------------ */
+/* instance, physical device, device, queue (icd_stubs.cpp, query.cpp)      */
+/* ------------------------------------------------------------------------ */
+
+static VkPhysicalDevice_T g_phys;
+
+VISOR_EXPORT VkResult vkCreateInstance(const VkInstanceCreateInfo *, const VkAllocationCallbacks *,
+                                       VkInstance *pInstance)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return vr(rc);
+  VkInstance_T *i = mk<VkInstance_T>();
+  set_magic(i);
+  set_magic(&g_phys);
+  *pInstance = i;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyInstance(VkInstance instance, const VkAllocationCallbacks *) { delete instance; }
+
+VISOR_EXPORT VkResult vkEnumerateInstanceVersion(uint32_t *pApiVersion)
+{
+  if(!pApiVersion)
+    return VK_ERROR_INITIALIZATION_FAILED;
+  *pApiVersion = VK_MAKE_VERSION(1, 0, 0);
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkEnumerateInstanceExtensionProperties(const char *, uint32_t *pCount,
+                                                             VkExtensionProperties *)
+{
+  /* headless: no surface extensions (WSI is replaced by mapped render targets) */
+  if(pCount)
+    *pCount = 0;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkEnumerateDeviceExtensionProperties(VkPhysicalDevice, const char *, uint32_t *pCount,
+                                                           VkExtensionProperties *)
+{
+  if(pCount)
+    *pCount = 0;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkEnumeratePhysicalDevices(VkInstance, uint32_t *pCount, VkPhysicalDevice *pDevs)
+{
+  if(!pDevs)
+  {
+    *pCount = 1;
+    return VK_SUCCESS;
+  }
+  if(*pCount < 1)
+    return VK_INCOMPLETE;
+  set_magic(&g_phys);
+  pDevs[0] = &g_phys;
+  *pCount = 1;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkGetPhysicalDeviceFeatures(VkPhysicalDevice, VkPhysicalDeviceFeatures *f)
+{
+  memset(f, 0, sizeof(*f));
+  f->fullDrawIndexUint32 = VK_TRUE;
+  f->textureCompressionBC = VK_FALSE;
+}
+
+VISOR_EXPORT void vkGetPhysicalDeviceProperties(VkPhysicalDevice, VkPhysicalDeviceProperties *p)
+{
+  memset(p, 0, sizeof(*p));
+  vgpu_device_info info;
+  memset(&info, 0, sizeof(info));
+  vgpu_device_info_get(&info);
+  p->apiVersion = VK_MAKE_VERSION(1, 0, 47);
+  p->driverVersion = VK_MAKE_VERSION(0, 1, 0);
+  p->vendorID = 0x10DE;
+  p->deviceType = VK_PHYSICAL_DEVICE_TYPE_DISCRETE_GPU;
+  snprintf(p->deviceName, sizeof(p->deviceName), "Visor GB300 (%s)", info.name);
+  VkPhysicalDeviceLimits &l = p->limits;
+  l.maxImageDimension1D = l.maxImageDimension2D = 16384;
+  l.maxImageDimension3D = 2048;
+  l.maxImageDimensionCube = 16384;
+  l.maxImageArrayLayers = 2048;
+  l.maxUniformBufferRange = 65536;
+  l.maxStorageBufferRange = 1u << 30;
+  l.maxPushConstantsSize = 128;
+  l.maxMemoryAllocationCount = 1u << 20;
+  l.maxSamplerAllocationCount = 4000;
+  l.bufferImageGranularity = 256;
+  l.maxBoundDescriptorSets = 8;
+  l.maxPerStageDescriptorSamplers = VGX_MAX_TEX;
+  l.maxPerStageDescriptorUniformBuffers = VGX_MAX_UBO;
+  l.maxPerStageDescriptorSampledImages = VGX_MAX_TEX;
+  l.maxPerStageResources = VGX_MAX_TEX + VGX_MAX_UBO;
+  l.maxDescriptorSetSamplers = VGX_MAX_TEX;
+  l.maxDescriptorSetUniformBuffers = VGX_MAX_UBO;
+  l.maxDescriptorSetSampledImages = VGX_MAX_TEX;
+  l.maxVertexInputAttributes = VGX_MAX_ATTRS;
+  l.maxVertexInputBindings = VGX_MAX_VB;
+  l.maxVertexInputAttributeOffset = 2047;
+  l.maxVertexInputBindingStride = 2048;
+  l.maxVertexOutputComponents = 64;
+  l.maxFragmentInputComponents = 64;
+  l.maxFragmentOutputAttachments = 1;
+  l.maxFragmentCombinedOutputResources = 1;
+  l.maxDrawIndexedIndexValue = 0xffffffffu;
+  l.maxViewports = 1;
+  l.maxViewportDimensions[0] = l.maxViewportDimensions[1] = 16384;
+  l.viewportBoundsRange[0] = -32768.0f;
+  l.viewportBoundsRange[1] = 32767.0f;
+  l.minMemoryMapAlignment = 64;
+  l.minTexelBufferOffsetAlignment = 16;
+  l.minUniformBufferOffsetAlignment = 16;
+  l.minStorageBufferOffsetAlignment = 16;
+  l.maxFramebufferWidth = l.maxFramebufferHeight = 16384;
+  l.maxFramebufferLayers = 1;
+  l.framebufferColorSampleCounts = l.framebufferDepthSampleCounts = VK_SAMPLE_COUNT_1_BIT;
+  l.framebufferNoAttachmentsSampleCounts = VK_SAMPLE_COUNT_1_BIT;
+  l.maxColorAttachments = 1;
+  l.sampledImageColorSampleCounts = l.sampledImageDepthSampleCounts = VK_SAMPLE_COUNT_1_BIT;
+  l.storageImageSampleCounts = VK_SAMPLE_COUNT_1_BIT;
+  l.timestampPeriod = 1.0f;
+  l.discreteQueuePriorities = 2;
+  l.pointSizeRange[0] = l.pointSizeRange[1] = 1.0f;
+  l.lineWidthRange[0] = l.lineWidthRange[1] = 1.0f;
+  l.optimalBufferCopyOffsetAlignment = 16;
+  l.optimalBufferCopyRowPitchAlignment = 16;
+  l.nonCoherentAtomSize = 64;
+}
+
+VISOR_EXPORT void vkGetPhysicalDeviceQueueFamilyProperties(VkPhysicalDevice, uint32_t *pCount,
+                                                           VkQueueFamilyProperties *props)
+{
+  if(!props)
+  {
+    *pCount = 1;
+    return;
+  }
+  memset(props, 0, sizeof(*props));
+  props->queueFlags = VK_QUEUE_GRAPHICS_BIT | VK_QUEUE_COMPUTE_BIT | VK_QUEUE_TRANSFER_BIT;
+  props->queueCount = 1;
+  props->timestampValidBits = 64;
+  props->minImageTransferGranularity.width = props->minImageTransferGranularity.height =
+      props->minImageTransferGranularity.depth = 1;
+  *pCount = 1;
+}
+
+VISOR_EXPORT void vkGetPhysicalDeviceMemoryProperties(VkPhysicalDevice, VkPhysicalDeviceMemoryProperties *p)
+{
+  /* the reference's two types (query.cpp:246-267), with the GPU's real heap size */
+  memset(p, 0, sizeof(*p));
+  vgpu_device_info info;
+  memset(&info, 0, sizeof(info));
+  vgpu_device_info_get(&info);
+  p->memoryHeapCount = 2;
+  p->memoryHeaps[0].flags = VK_MEMORY_HEAP_DEVICE_LOCAL_BIT;
+  p->memoryHeaps[0].size = info.total_memory ? info.total_memory : (1ull << 30);
+  p->memoryHeaps[1].flags = 0;
+  p->memoryHeaps[1].size = 64ull << 30;
+  p->memoryTypeCount = 2;
+  p->memoryTypes[0].propertyFlags = VK_MEMORY_PROPERTY_DEVICE_LOCAL_BIT;
+  p->memoryTypes[0].heapIndex = 0;
+  p->memoryTypes[1].propertyFlags = VK_MEMORY_PROPERTY_HOST_VISIBLE_BIT |
+                                    VK_MEMORY_PROPERTY_HOST_COHERENT_BIT |
+                                    VK_MEMORY_PROPERTY_HOST_CACHED_BIT;
+  p->memoryTypes[1].heapIndex = 1;
+}
+
+VISOR_EXPORT void vkGetPhysicalDeviceFormatProperties(VkPhysicalDevice, VkFormat format, VkFormatProperties *p)
+{
+  p->bufferFeatures = VK_FORMAT_FEATURE_VERTEX_BUFFER_BIT;
+  p->linearTilingFeatures = VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT |
+                            VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT;
+  if(format == VK_FORMAT_D32_SFLOAT || format == VK_FORMAT_D32_SFLOAT_S8_UINT)
+  {
+    p->bufferFeatures = 0;
+    p->linearTilingFeatures = VK_FORMAT_FEATURE_DEPTH_STENCIL_ATTACHMENT_BIT;
+  }
+  p->optimalTilingFeatures = p->linearTilingFeatures;
+}
+
+VISOR_EXPORT VkResult vkCreateDevice(VkPhysicalDevice, const VkDeviceCreateInfo *, const VkAllocationCallbacks *,
+                                     VkDevice *pDevice)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return vr(rc);
+  VkDevice_T *d = new VkDevice_T();
+  set_magic(d);
+  d->queue = new VkQueue_T();
+  set_magic(d->queue);
+  rc = vgpu_queue_create(&d->queue->q);
+  if(rc)
+  {
+    delete d->queue;
+    delete d;
+    return vr(rc);
+  }
+  *pDevice = d;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyDevice(VkDevice d, const VkAllocationCallbacks *)
+{
+  if(!d)
+    return;
+  vgpu_queue_destroy(d->queue->q);
+  for(auto &kv : d->programs)
+    vgpu_program_destroy(kv.second);
+  delete d->queue;
+  delete d;
+}
+
+VISOR_EXPORT void vkGetDeviceQueue(VkDevice d, uint32_t, uint32_t, VkQueue *pQueue) { *pQueue = d->queue; }
+
+/* ------------------------------------------------------------------------ */
+/* memory, buffers, images (memory.cpp, buffers.cpp, images.cpp)            */
+/* ------------------------------------------------------------------------ */
+
+VISOR_EXPORT VkResult vkAllocateMemory(VkDevice, const VkMemoryAllocateInfo *info, const VkAllocationCallbacks *,
+                                       VkDeviceMemory *pMem)
+{
+  VkDeviceMemory_T *m = new VkDeviceMemory_T();
+  m->size = info->allocationSize;
+  m->type = info->memoryTypeIndex;
+  int rc = vgpu_mem_alloc(m->size, m->type == 1, &m->dptr, &m->hptr);
+  if(rc)
+  {
+    delete m;
+    return vr(rc);
+  }
+  *pMem = m;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkFreeMemory(VkDevice, VkDeviceMemory m, const VkAllocationCallbacks *)
+{
+  if(!m)
+    return;
+  vgpu_mem_free(m->dptr, m->hptr);
+  delete m;
+}
+
+VISOR_EXPORT VkResult vkMapMemory(VkDevice, VkDeviceMemory m, VkDeviceSize offset, VkDeviceSize, VkMemoryMapFlags,
+                                  void **ppData)
+{
+  if(!m->hptr)
+    return VK_ERROR_MEMORY_MAP_FAILED;
+  *ppData = (uint8_t *)m->hptr + offset;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkUnmapMemory(VkDevice, VkDeviceMemory) {}
+
+VISOR_EXPORT VkResult vkFlushMappedMemoryRanges(VkDevice, uint32_t, const VkMappedMemoryRange *)
+{
+  return VK_SUCCESS; /* coherent: uploaded at submit */
+}
+
+VISOR_EXPORT VkResult vkCreateBuffer(VkDevice, const VkBufferCreateInfo *info, const VkAllocationCallbacks *,
+                                     VkBuffer *pBuffer)
+{
+  VkBuffer_T *b = new VkBuffer_T();
+  b->size = info->size;
+  *pBuffer = b;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyBuffer(VkDevice, VkBuffer b, const VkAllocationCallbacks *) { delete b; }
+
+VISOR_EXPORT void vkGetBufferMemoryRequirements(VkDevice, VkBuffer b, VkMemoryRequirements *r)
+{
+  r->size = (b->size + 255) & ~255ull;
+  r->alignment = 256;
+  r->memoryTypeBits = 0x3;
+}
+
+VISOR_EXPORT VkResult vkBindBufferMemory(VkDevice, VkBuffer b, VkDeviceMemory m, VkDeviceSize off)
+{
+  b->mem = m;
+  b->offset = off;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkCreateImage(VkDevice, const VkImageCreateInfo *info, const VkAllocationCallbacks *,
+                                    VkImage *pImage)
+{
+  VkImage_T *i = new VkImage_T();
+  i->extent = info->extent;
+  i->format = info->format;
+  i->mips = info->mipLevels ? info->mipLevels : 1;
+  i->layers = info->arrayLayers ? info->arrayLayers : 1;
+  i->bpp = format_bpp(info->format);
+  *pImage = i;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyImage(VkDevice, VkImage i, const VkAllocationCallbacks *) { delete i; }
+
+VISOR_EXPORT void vkGetImageMemoryRequirements(VkDevice, VkImage i, VkMemoryRequirements *r)
+{
+  VkDeviceSize sz = subresource_offset(i, 0, i->layers);
+  if(i->extent.depth > 1)
+    sz *= i->extent.depth;
+  r->size = (sz + 255) & ~255ull;
+  r->alignment = 256;
+  r->memoryTypeBits = 0x3;
+}
+
+VISOR_EXPORT VkResult vkBindImageMemory(VkDevice, VkImage i, VkDeviceMemory m, VkDeviceSize off)
+{
+  i->mem = m;
+  i->offset = off;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkGetImageSubresourceLayout(VkDevice, VkImage i, const VkImageSubresource *s, VkSubresourceLayout *l)
+{
+  l->offset = subresource_offset(i, s->mipLevel, s->arrayLayer);
+  uint32_t w = std::max(1u, i->extent.width >> s->mipLevel), h = std::max(1u, i->extent.height >> s->mipLevel);
+  l->rowPitch = (VkDeviceSize)w * i->bpp;
+  l->arrayPitch = l->depthPitch = l->size = (VkDeviceSize)w * h * i->bpp;
+}
+
+VISOR_EXPORT VkResult vkCreateImageView(VkDevice, const VkImageViewCreateInfo *info, const VkAllocationCallbacks *,
+                                        VkImageView *pView)
+{
+  VkImageView_T *v = new VkImageView_T();
+  v->image = info->image;
+  v->base_mip = info->subresourceRange.baseMipLevel;
+  v->levels = info->subresourceRange.levelCount;
+  if(v->levels == ~0u || v->levels == 0)
+    v->levels = v->image->mips - v->base_mip;
+  *pView = v;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyImageView(VkDevice, VkImageView v, const VkAllocationCallbacks *) { delete v; }
+
+VISOR_EXPORT VkResult vkCreateSampler(VkDevice, const VkSamplerCreateInfo *info, const VkAllocationCallbacks *,
+                                      VkSampler *pSampler)
+{
+  /* The reference ignores samplers (bilinear, repeat, mip 0).  This path keeps
+     that unless the sampler asks for linear mipmapping over a mip chain
+     (trilinear) or nearest filtering in both directions. */
+  VkSampler_T *s = new VkSampler_T();
+  if(info->mipmapMode == VK_SAMPLER_MIPMAP_MODE_LINEAR && info->maxLod > 0.0f &&
+     info->minFilter == VK_FILTER_LINEAR)
+    s->filter = VGX_FILTER_TRILINEAR;
+  else if(info->magFilter == VK_FILTER_NEAREST && info->minFilter == VK_FILTER_NEAREST)
+    s->filter = VGX_FILTER_NEAREST;
+  *pSampler = s;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroySampler(VkDevice, VkSampler s, const VkAllocationCallbacks *) { delete s; }
+
+/* ------------------------------------------------------------------------ */
+/* descriptors, render passes, framebuffers (descriptors.cpp, renderpass.cpp) */
+/* ------------------------------------------------------------------------ */
+
+VISOR_EXPORT VkResult vkCreateDescriptorSetLayout(VkDevice, const VkDescriptorSetLayoutCreateInfo *info,
+                                                  const VkAllocationCallbacks *, VkDescriptorSetLayout *p)
+{
+  VkDescriptorSetLayout_T *l = new VkDescriptorSetLayout_T();
+  l->bindings = info->bindingCount;
+  *p = l;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyDescriptorSetLayout(VkDevice, VkDescriptorSetLayout l, const VkAllocationCallbacks *)
+{
+  delete l;
+}
+
+VISOR_EXPORT VkResult vkCreatePipelineLayout(VkDevice, const VkPipelineLayoutCreateInfo *, const VkAllocationCallbacks *,
+                                             VkPipelineLayout *p)
+{
+  *p = new VkPipelineLayout_T();
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyPipelineLayout(VkDevice, VkPipelineLayout l, const VkAllocationCallbacks *) { delete l; }
+
+VISOR_EXPORT VkResult vkCreateDescriptorPool(VkDevice, const VkDescriptorPoolCreateInfo *, const VkAllocationCallbacks *,
+                                             VkDescriptorPool *p)
+{
+  *p = new VkDescriptorPool_T();
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyDescriptorPool(VkDevice, VkDescriptorPool p, const VkAllocationCallbacks *) { delete p; }
+
+VISOR_EXPORT VkResult vkAllocateDescriptorSets(VkDevice, const VkDescriptorSetAllocateInfo *info, VkDescriptorSet *sets)
+{
+  /* every requested set is written (the reference writes only pDescriptorSets[0]) */
+  for(uint32_t i = 0; i < info->descriptorSetCount; i++)
+    sets[i] = new VkDescriptorSet_T();
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkFreeDescriptorSets(VkDevice, VkDescriptorPool, uint32_t n, const VkDescriptorSet *sets)
+{
+  for(uint32_t i = 0; i < n; i++)
+    delete sets[i];
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkUpdateDescriptorSets(VkDevice, uint32_t nw, const VkWriteDescriptorSet *w, uint32_t nc,
+                                         const VkCopyDescriptorSet *c)
+{
+  for(uint32_t i = 0; i < nw; i++)
+  {
+    VkDescriptorSet_T::Bind &b = w[i].dstSet->binds[w[i].dstBinding];
+    b.type = w[i].descriptorType;
+    switch(w[i].descriptorType)
+    {
+      case VK_DESCRIPTOR_TYPE_SAMPLER:
+      case VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER:
+      case VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE:
+      case VK_DESCRIPTOR_TYPE_STORAGE_IMAGE:
+      case VK_DESCRIPTOR_TYPE_INPUT_ATTACHMENT:
+        if(w[i].pImageInfo[0].imageView)
+          b.view = w[i].pImageInfo[0].imageView;
+        if(w[i].pImageInfo[0].sampler)
+          b.sampler = w[i].pImageInfo[0].sampler;
+        break;
+      case VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER:
+      case VK_DESCRIPTOR_TYPE_STORAGE_BUFFER:
+      case VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC:
+      case VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC:
+        b.buffer = w[i].pBufferInfo[0].buffer;
+        b.offset = w[i].pBufferInfo[0].offset;
+        b.range = w[i].pBufferInfo[0].range;
+        break;
+      default: break;
+    }
+  }
+  for(uint32_t i = 0; i < nc; i++)
+    for(uint32_t k = 0; k < c[i].descriptorCount; k++)
+      c[i].dstSet->binds[c[i].dstBinding + k] = c[i].srcSet->binds[c[i].srcBinding + k];
+}
+
+VISOR_EXPORT VkResult vkCreateRenderPass(VkDevice, const VkRenderPassCreateInfo *info, const VkAllocationCallbacks *,
+                                         VkRenderPass *p)
+{
+  /* subpass 0: colour attachment 0 and the depth attachment (renderpass.cpp:22-52) */
+  VkRenderPass_T *rp = new VkRenderPass_T();
+  if(info->subpassCount > 0)
+  {
+    const VkSubpassDescription &s = info->pSubpasses[0];
+    if(s.colorAttachmentCount > 0 && s.pColorAttachments[0].attachment != VK_ATTACHMENT_UNUSED)
+    {
+      rp->color = (int32_t)s.pColorAttachments[0].attachment;
+      rp->color_clear = info->pAttachments[rp->color].loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR;
+    }
+    if(s.pDepthStencilAttachment && s.pDepthStencilAttachment->attachment != VK_ATTACHMENT_UNUSED)
+    {
+      rp->depth = (int32_t)s.pDepthStencilAttachment->attachment;
+      rp->depth_clear = info->pAttachments[rp->depth].loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR;
+    }
+  }
+  *p = rp;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyRenderPass(VkDevice, VkRenderPass rp, const VkAllocationCallbacks *) { delete rp; }
+
+VISOR_EXPORT VkResult vkCreateFramebuffer(VkDevice, const VkFramebufferCreateInfo *info, const VkAllocationCallbacks *,
+                                          VkFramebuffer *p)
+{
+  VkFramebuffer_T *f = new VkFramebuffer_T();
+  f->views.assign(info->pAttachments, info->pAttachments + info->attachmentCount);
+  *p = f;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyFramebuffer(VkDevice, VkFramebuffer f, const VkAllocationCallbacks *) { delete f; }
+
+/* ------------------------------------------------------------------------ */
+/* shaders and pipelines (shaders.cpp)                                      */
+/* ------------------------------------------------------------------------ */
+
+VISOR_EXPORT VkResult vkCreateShaderModule(VkDevice, const VkShaderModuleCreateInfo *info, const VkAllocationCallbacks *,
+                                           VkShaderModule *p)
+{
+  std::string err;
+  vst::Module *m = vst::parse(info->pCode, info->codeSize / 4, err);
+  if(!m)
+  {
+    fprintf(stderr, "visor_gb300: shader module rejected: %s\n", err.c_str());
+    /* the reference reports compile failure as VK_ERROR_DEVICE_LOST (shaders.cpp:13-14) */
+    return VK_ERROR_DEVICE_LOST;
+  }
+  VkShaderModule_T *s = new VkShaderModule_T();
+  s->mod = m;
+  *p = s;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyShaderModule(VkDevice, VkShaderModule s, const VkAllocationCallbacks *)
+{
+  if(!s)
+    return;
+  vst::destroy(s->mod);
+  delete s;
+}
+
+VISOR_EXPORT VkResult vkCreatePipelineCache(VkDevice, const VkPipelineCacheCreateInfo *, const VkAllocationCallbacks *,
+                                            VkPipelineCache *p)
+{
+  *p = new VkPipelineCache_T();
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyPipelineCache(VkDevice, VkPipelineCache c, const VkAllocationCallbacks *) { delete c; }
+
+static uint32_t attr_format(VkFormat f)
+{
+  switch(f)
+  {
+    case VK_FORMAT_R32G32B32A32_SFLOAT: case VK_FORMAT_R32G32B32A32_UINT: case VK_FORMAT_R32G32B32A32_SINT:
+      return VGX_FMT_RGBA32;
+    case VK_FORMAT_R32G32B32_SFLOAT: case VK_FORMAT_R32G32B32_UINT: case VK_FORMAT_R32G32B32_SINT:
+      return VGX_FMT_RGB32;
+    case VK_FORMAT_R32G32_SFLOAT: case VK_FORMAT_R32G32_UINT: case VK_FORMAT_R32G32_SINT:
+      return VGX_FMT_RG32;
+    case VK_FORMAT_R32_SFLOAT: case VK_FORMAT_R32_UINT: case VK_FORMAT_R32_SINT: return VGX_FMT_R32;
+    case VK_FORMAT_R8G8B8A8_UNORM: return VGX_FMT_RGBA8_UNORM;
+    default: return VGX_FMT_NONE;
+  }
+}
+
+VISOR_EXPORT VkResult vkCreateGraphicsPipelines(VkDevice dev, VkPipelineCache, uint32_t n,
+                                                const VkGraphicsPipelineCreateInfo *infos,
+                                                const VkAllocationCallbacks *, VkPipeline *out)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    const VkGraphicsPipelineCreateInfo &ci = infos[i];
+    VkPipeline_T *p = new VkPipeline_T();
+    const VkPipelineVertexInputStateCreateInfo *vi = ci.pVertexInputState;
+    uint32_t strides[16] = {0};
+    for(uint32_t b = 0; vi && b < vi->vertexBindingDescriptionCount; b++)
+      if(vi->pVertexBindingDescriptions[b].binding < 16)
+        strides[vi->pVertexBindingDescriptions[b].binding] = vi->pVertexBindingDescriptions[b].stride;
+    for(uint32_t a = 0; vi && a < vi->vertexAttributeDescriptionCount; a++)
+    {
+      const VkVertexInputAttributeDescription &d = vi->pVertexAttributeDescriptions[a];
+      if(d.location >= VGX_MAX_ATTRS || d.binding >= VGX_MAX_VB)
+        continue;
+      p->attrs[d.location].format = attr_format(d.format);
+      p->attrs[d.location].binding = d.binding;
+      p->attrs[d.location].offset = d.offset;
+    }
+    for(uint32_t b = 0; b < VGX_MAX_VB; b++)
+      p->strides[b] = strides[b];
+    p->topology = ci.pInputAssemblyState ? ci.pInputAssemblyState->topology : 3;
+    if(ci.pRasterizationState)
+    {
+      p->cull = ci.pRasterizationState->cullMode;
+      p->front = ci.pRasterizationState->frontFace;
+    }
+    if(ci.pDepthStencilState)
+    {
+      p->depth_op = ci.pDepthStencilState->depthCompareOp;
+      p->depth_write = ci.pDepthStencilState->depthWriteEnable == VK_TRUE;
+    }
+    if(ci.pColorBlendState && ci.pColorBlendState->attachmentCount > 0)
+    {
+      const VkPipelineColorBlendAttachmentState &a = ci.pColorBlendState->pAttachments[0];
+      p->blend = a.blendEnable ? 1 : 0;
+      p->src = a.srcColorBlendFactor;
+      p->dst = a.dstColorBlendFactor;
+      p->op = a.colorBlendOp;
+    }
+    const vst::Module *vs = nullptr, *fs = nullptr;
+    const char *vs_name = "main", *fs_name = "main";
+    for(uint32_t s = 0; s < ci.stageCount; s++)
+    {
+      if(ci.pStages[s].stage == VK_SHADER_STAGE_VERTEX_BIT)
+      {
+        vs = ci.pStages[s].module->mod;
+        vs_name = ci.pStages[s].pName;
+      }
+      else if(ci.pStages[s].stage == VK_SHADER_STAGE_FRAGMENT_BIT)
+      {
+        fs = ci.pStages[s].module->mod;
+        fs_name = ci.pStages[s].pName;
+      }
+    }
+    std::string err;
+    if(!vs || !fs || !vst::translate(vs, vs_name, fs, fs_name, p->tr, err))
+    {
+      fprintf(stderr, "visor_gb300: pipeline translation failed: %s\n", err.c_str());
+      delete p;
+      for(uint32_t k = 0; k < i; k++)
+        out[k] = VK_NULL_HANDLE;
+      return VK_ERROR_INITIALIZATION_FAILED;
+    }
+    {
+      std::lock_guard<std::mutex> lk(dev->mu);
+      auto it = dev->programs.find(p->tr.source);
+      if(it != dev->programs.end())
+        p->prog = it->second;
+    }
+    if(!p->prog)
+    {
+      char log[4096] = {0};
+      int rc = vgpu_program_create(p->tr.source.c_str(), 3, &p->prog, log, sizeof(log));
+      if(rc)
+      {
+        delete p;
+        return vr(rc);
+      }
+      std::lock_guard<std::mutex> lk(dev->mu);
+      dev->programs[p->tr.source] = p->prog;
+    }
+    out[i] = p;
+  }
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkCreateComputePipelines(VkDevice, VkPipelineCache, uint32_t n, const VkComputePipelineCreateInfo *,
+                                               const VkAllocationCallbacks *, VkPipeline *out)
+{
+  for(uint32_t i = 0; i < n; i++)
+    out[i] = new VkPipeline_T();
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyPipeline(VkDevice, VkPipeline p, const VkAllocationCallbacks *) { delete p; }
+
+/* ------------------------------------------------------------------------ */
+/* fences, semaphores                                                        */
+/* ------------------------------------------------------------------------ */
+
+VISOR_EXPORT VkResult vkCreateFence(VkDevice, const VkFenceCreateInfo *info, const VkAllocationCallbacks *, VkFence *p)
+{
+  VkFence_T *f = new VkFence_T();
+  int rc = vgpu_fence_create(&f->f);
+  if(rc)
+  {
+    delete f;
+    return vr(rc);
+  }
+  f->signaled = info && (info->flags & VK_FENCE_CREATE_SIGNALED_BIT);
+  *p = f;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroyFence(VkDevice, VkFence f, const VkAllocationCallbacks *)
+{
+  if(!f)
+    return;
+  vgpu_fence_destroy(f->f);
+  delete f;
+}
+
+VISOR_EXPORT VkResult vkResetFences(VkDevice, uint32_t n, const VkFence *fs)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    vgpu_fence_reset(fs[i]->f);
+    fs[i]->signaled = false;
+  }
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkWaitForFences(VkDevice, uint32_t n, const VkFence *fs, VkBool32 all, uint64_t timeout)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    int rc = vgpu_fence_wait(fs[i]->f, timeout);
+    if(rc == VGPU_OK && !all)
+      return VK_SUCCESS;
+    if(rc != VGPU_OK)
+      return vr(rc);
+  }
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkCreateSemaphore(VkDevice, const VkSemaphoreCreateInfo *, const VkAllocationCallbacks *, VkSemaphore *p)
+{
+  *p = new VkSemaphore_T();
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroySemaphore(VkDevice, VkSemaphore s, const VkAllocationCallbacks *) { delete s; }
+
+VISOR_EXPORT VkResult vkDeviceWaitIdle(VkDevice d) { return vr(vgpu_queue_wait_idle(d->queue->q)); }
+VISOR_EXPORT VkResult vkQueueWaitIdle(VkQueue q) { return vr(vgpu_queue_wait_idle(q->q)); }
+
+/* ------------------------------------------------------------------------ */
+/* command pools and recording (cmd_alloc.cpp, cmd_record.cpp)              */
+/* ------------------------------------------------------------------------ */
+
+VISOR_EXPORT VkResult vkCreateCommandPool(VkDevice, const VkCommandPoolCreateInfo *, const VkAllocationCallbacks *,
+                                          VkCommandPool *p)
+{
+  *p = new VkCommandPool_T();
+  return VK_SUCCESS;
+}
+
+static void cb_free(VkCommandBuffer c)
+{
+  vgpu_list_destroy(c->list);
+  delete c;
+}
+
+VISOR_EXPORT void vkDestroyCommandPool(VkDevice, VkCommandPool p, const VkAllocationCallbacks *)
+{
+  if(!p)
+    return;
+  for(VkCommandBuffer c : p->buffers)
+    cb_free(c);
+  delete p;
+}
+
+VISOR_EXPORT VkResult vkAllocateCommandBuffers(VkDevice, const VkCommandBufferAllocateInfo *info, VkCommandBuffer *out)
+{
+  for(uint32_t i = 0; i < info->commandBufferCount; i++)
+  {
+    VkCommandBuffer_T *c = new VkCommandBuffer_T();
+    set_magic(c);
+    c->pool = info->commandPool;
+    info->commandPool->buffers.push_back(c);
+    out[i] = c;
+  }
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkFreeCommandBuffers(VkDevice, VkCommandPool p, uint32_t n, const VkCommandBuffer *cbs)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    auto &v = p->buffers;
+    v.erase(std::remove(v.begin(), v.end(), cbs[i]), v.end());
+    cb_free(cbs[i]);
+  }
+}
+
+VISOR_EXPORT VkResult vkBeginCommandBuffer(VkCommandBuffer c, const VkCommandBufferBeginInfo *)
+{
+  c->stream.clear();
+  vgpu_list_destroy(c->list);
+  c->list = nullptr;
+  c->lowered = false;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult vkEndCommandBuffer(VkCommandBuffer) { return VK_SUCCESS; }
+
+namespace pk
+{
+struct BeginRP
+{
+  VkRenderPass rp;
+  VkFramebuffer fb;
+  VkClearValue clear[8];
+};
+struct BindPipeline
+{
+  VkPipeline p;
+};
+struct BindSet
+{
+  uint32_t idx;
+  VkDescriptorSet set;
+};
+struct BindVB
+{
+  uint32_t slot;
+  VkBuffer buf;
+  VkDeviceSize off;
+};
+struct BindIB
+{
+  VkBuffer buf;
+  VkDeviceSize off;
+  VkIndexType type;
+};
+struct Push
+{
+  uint32_t off, size;
+  uint8_t data[128];
+};
+struct Draw
+{
+  uint32_t count, instances, first, first_instance;
+  int32_t vertex_offset;
+};
+struct CopyBuf2Img
+{
+  VkBuffer src;
+  VkImage dst;
+  VkBufferImageCopy region;
+};
+struct CopyBuf
+{
+  VkBuffer src, dst;
+  VkBufferCopy region;
+};
+struct Viewport
+{
+  VkViewport v;
+};
+}    // namespace pk
+
+VISOR_EXPORT void vkCmdPipelineBarrier(VkCommandBuffer c, VkPipelineStageFlags, VkPipelineStageFlags, VkDependencyFlags,
+                                       uint32_t, const VkMemoryBarrier *, uint32_t, const VkBufferMemoryBarrier *,
+                                       uint32_t, const VkImageMemoryBarrier *)
+{
+  c->push(Pkt::Barrier);
+}
+
+VISOR_EXPORT void vkCmdBeginRenderPass(VkCommandBuffer c, const VkRenderPassBeginInfo *info, VkSubpassContents)
+{
+  pk::BeginRP b;
+  memset(&b, 0, sizeof(b));
+  b.rp = info->renderPass;
+  b.fb = info->framebuffer;
+  memcpy(b.clear, info->pClearValues, sizeof(VkClearValue) * std::min(info->clearValueCount, 8u));
+  c->push(Pkt::BeginRP, b);
+}
+
+VISOR_EXPORT void vkCmdEndRenderPass(VkCommandBuffer c) { c->push(Pkt::EndRP); }
+
+VISOR_EXPORT void vkCmdBindPipeline(VkCommandBuffer c, VkPipelineBindPoint, VkPipeline p)
+{
+  pk::BindPipeline b = {p};
+  c->push(Pkt::BindPipeline, b);
+}
+
+VISOR_EXPORT void vkCmdBindDescriptorSets(VkCommandBuffer c, VkPipelineBindPoint, VkPipelineLayout, uint32_t first,
+                                          uint32_t n, const VkDescriptorSet *sets, uint32_t, const uint32_t *)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    pk::BindSet b = {first + i, sets[i]};
+    c->push(Pkt::BindSet, b);
+  }
+}
+
+VISOR_EXPORT void vkCmdBindVertexBuffers(VkCommandBuffer c, uint32_t first, uint32_t n, const VkBuffer *bufs,
+                                         const VkDeviceSize *offs)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    pk::BindVB b = {first + i, bufs[i], offs[i]};
+    c->push(Pkt::BindVB, b);
+  }
+}
+
+VISOR_EXPORT void vkCmdBindIndexBuffer(VkCommandBuffer c, VkBuffer buf, VkDeviceSize off, VkIndexType type)
+{
+  pk::BindIB b = {buf, off, type};
+  c->push(Pkt::BindIB, b);
+}
+
+VISOR_EXPORT void vkCmdSetViewport(VkCommandBuffer c, uint32_t, uint32_t, const VkViewport *v)
+{
+  pk::Viewport b = {v[0]};
+  c->push(Pkt::SetViewport, b);
+}
+
+VISOR_EXPORT void vkCmdSetScissor(VkCommandBuffer c, uint32_t, uint32_t, const VkRect2D *) { c->push(Pkt::SetScissor); }
+
+VISOR_EXPORT void vkCmdPushConstants(VkCommandBuffer c, VkPipelineLayout, VkShaderStageFlags, uint32_t off,
+                                     uint32_t size, const void *data)
+{
+  pk::Push b;
+  memset(&b, 0, sizeof(b));
+  b.off = off;
+  b.size = std::min<uint32_t>(size, 128 - std::min<uint32_t>(off, 128));
+  memcpy(b.data, data, b.size);
+  c->push(Pkt::Push, b);
+}
+
+VISOR_EXPORT void vkCmdDraw(VkCommandBuffer c, uint32_t count, uint32_t instances, uint32_t first, uint32_t first_instance)
+{
+  pk::Draw b = {count, instances, first, first_instance, 0};
+  c->push(Pkt::Draw, b);
+}
+
+VISOR_EXPORT void vkCmdDrawIndexed(VkCommandBuffer c, uint32_t count, uint32_t instances, uint32_t first,
+                                   int32_t vertex_offset, uint32_t first_instance)
+{
+  pk::Draw b = {count, instances, first, first_instance, vertex_offset};
+  c->push(Pkt::DrawIndexed, b);
+}
+
+VISOR_EXPORT void vkCmdCopyBufferToImage(VkCommandBuffer c, VkBuffer src, VkImage dst, VkImageLayout, uint32_t n,
+                                         const VkBufferImageCopy *regions)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    pk::CopyBuf2Img b = {src, dst, regions[i]};
+    c->push(Pkt::CopyBuf2Img, b);
+  }
+}
+
+VISOR_EXPORT void vkCmdCopyBuffer(VkCommandBuffer c, VkBuffer src, VkBuffer dst, uint32_t n, const VkBufferCopy *regions)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    pk::CopyBuf b = {src, dst, regions[i]};
+    c->push(Pkt::CopyBuf, b);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* lowering and submission (cmd_exec.cpp)                                   */
+/* ------------------------------------------------------------------------ */
+
+namespace
+{
+struct ReplayState
+{
+  VkPipeline_T *pipeline = nullptr;
+  VkDescriptorSet_T *sets[8] = {};
+  struct
+  {
+    VkBuffer_T *buf = nullptr;
+    VkDeviceSize off = 0;
+  } vbs[VGX_MAX_VB];
+  VkBuffer_T *ib = nullptr;
+  VkDeviceSize ib_off = 0;
+  VkIndexType ib_type = VK_INDEX_TYPE_UINT32;
+  VkImageView_T *col = nullptr, *depth = nullptr;
+  uint8_t push[128] = {};
+  VgxTarget target;
+};
+
+void note_read(std::map<VkDeviceMemory_T *, int> &use, VkDeviceMemory_T *m)
+{
+  if(m && m->hptr)
+    use[m] |= 1;
+}
+void note_write(std::map<VkDeviceMemory_T *, int> &use, VkDeviceMemory_T *m)
+{
+  if(m && m->hptr)
+    use[m] |= 2;
+}
+
+uint32_t clear_bgra(const VkClearColorValue &c)
+{
+  /* ClearTarget (rasterizer.cpp:332-361): byte(f * 255.0f) into B,G,R,A order */
+  uint8_t e[4];
+  e[2] = (uint8_t)(c.float32[0] * 255.0f);
+  e[1] = (uint8_t)(c.float32[1] * 255.0f);
+  e[0] = (uint8_t)(c.float32[2] * 255.0f);
+  e[3] = (uint8_t)(c.float32[3] * 255.0f);
+  uint32_t v;
+  memcpy(&v, e, 4);
+  return v;
+}
+
+void fill_texture(VgxTex &t, VkDescriptorSet_T::Bind *b)
+{
+  memset(&t, 0, sizeof(t));
+  if(!b || !b->view || !b->view->image || !b->view->image->mem)
+    return;
+  VkImage_T *img = b->view->image;
+  uint32_t base = b->view->base_mip;
+  t.base = (u64)dev_addr(img->mem, img->offset + subresource_offset(img, base, 0));
+  t.width = std::max(1u, img->extent.width >> base);
+  t.height = std::max(1u, img->extent.height >> base);
+  t.mips = std::min<uint32_t>(std::max(1u, b->view->levels), VGX_MAX_MIPS);
+  t.filter = b->sampler ? b->sampler->filter : VGX_FILTER_REFERENCE;
+  u64 off = 0;
+  for(uint32_t m = 0; m < t.mips; m++)
+  {
+    t.mip_offset[m] = (u32)off;
+    off += (u64)std::max(1u, t.width >> m) * std::max(1u, t.height >> m) * img->bpp;
+  }
+}
+
+/* Replay the packet stream into a vgpu list (cmd_exec.cpp:15-185). */
+void lower(VkCommandBuffer c)
+{
+  vgpu_list *l = vgpu_list_create();
+  vgpu_list_set_mode(l, c->mode >= 0 ? c->mode : default_mode());
+  ReplayState s;
+  std::map<VkDeviceMemory_T *, int> use;
+  const uint8_t *cur = c->stream.data(), *end = cur + c->stream.size();
+  auto pull = [&](void *dst, size_t n) {
+    memcpy(dst, cur, n);
+    cur += n;
+  };
+  bool have_target = false;
+  while(cur < end)
+  {
+    Pkt k;
+    pull(&k, sizeof(k));
+    switch(k)
+    {
+      case Pkt::Barrier: case Pkt::SetScissor: break;
+      case Pkt::SetViewport:
+      {
+        pk::Viewport b;
+        pull(&b, sizeof(b));
+        break;
+      }
+      case Pkt::BeginRP:
+      {
+        pk::BeginRP b;
+        pull(&b, sizeof(b));
+        int ci = 0;
+        s.col = b.rp->color >= 0 ? b.fb->views[b.rp->color] : nullptr;
+        bool ccl = false, dcl = false;
+        uint32_t cbgra = 0;
+        float cdepth = 1.0f;
+        if(s.col && b.rp->color_clear)
+        {
+          ccl = true;
+          cbgra = clear_bgra(b.clear[ci++].color);
+        }
+        if(b.rp->depth >= 0)
+        {
+          s.depth = b.fb->views[b.rp->depth];
+          if(b.rp->depth_clear)
+          {
+            dcl = true;
+            cdepth = b.clear[ci++].depthStencil.depth;
+          }
+        }
+        have_target = s.col && s.col->image && s.col->image->mem;
+        if(have_target)
+        {
+          VgxTarget &t = s.target;
+          memset(&t, 0, sizeof(t));
+          VkImage_T *ci_ = s.col->image;
+          t.color = (u64)dev_addr(ci_->mem, ci_->offset);
+          t.width = (i32)ci_->extent.width;
+          t.height = (i32)ci_->extent.height;
+          t.depth = (s.depth && s.depth->image && s.depth->image->mem)
+                        ? (u64)dev_addr(s.depth->image->mem, s.depth->image->offset)
+                        : 0;
+          t.clear_bgra = cbgra;
+          t.clear_depth = cdepth;
+          if(ccl || dcl)
+            vgpu_list_clear(l, &t, ccl ? 1 : 0, dcl ? 1 : 0);
+          if(ccl)
+            note_write(use, ci_->mem);
+          else
+            note_read(use, ci_->mem), note_write(use, ci_->mem);
+          if(s.depth && s.depth->image)
+          {
+            if(dcl)
+              note_write(use, s.depth->image->mem);
+            else
+              note_read(use, s.depth->image->mem), note_write(use, s.depth->image->mem);
+          }
+        }
+        break;
+      }
+      case Pkt::EndRP:
+        s.col = nullptr; /* depth stays bound, as cmd_exec.cpp:65-72 */
+        have_target = false;
+        break;
+      case Pkt::BindPipeline:
+      {
+        pk::BindPipeline b;
+        pull(&b, sizeof(b));
+        s.pipeline = b.p;
+        break;
+      }
+      case Pkt::BindSet:
+      {
+        pk::BindSet b;
+        pull(&b, sizeof(b));
+        if(b.idx < 8)
+          s.sets[b.idx] = b.set;
+        break;
+      }
+      case Pkt::BindVB:
+      {
+        pk::BindVB b;
+        pull(&b, sizeof(b));
+        if(b.slot < VGX_MAX_VB)
+        {
+          s.vbs[b.slot].buf = b.buf;
+          s.vbs[b.slot].off = b.off;
+        }
+        break;
+      }
+      case Pkt::BindIB:
+      {
+        pk::BindIB b;
+        pull(&b, sizeof(b));
+        s.ib = b.buf;
+        s.ib_off = b.off;
+        s.ib_type = b.type;
+        break;
+      }
+      case Pkt::Push:
+      {
+        pk::Push b;
+        pull(&b, sizeof(b));
+        memcpy(s.push + b.off, b.data, b.size);
+        break;
+      }
+      case Pkt::Draw:
+      case Pkt::DrawIndexed:
+      {
+        pk::Draw b;
+        pull(&b, sizeof(b));
+        VkPipeline_T *p = s.pipeline;
+        if(!p || !have_target)
+          break;
+        VgxDraw d;
+        memset(&d, 0, sizeof(d));
+        for(int v = 0; v < VGX_MAX_VB; v++)
+          if(s.vbs[v].buf && s.vbs[v].buf->mem)
+          {
+            VkBuffer_T *vb = s.vbs[v].buf;
+            d.vb[v] = (u64)dev_addr(vb->mem, vb->offset + s.vbs[v].off);
+            d.vb_bytes[v] = vb->size > s.vbs[v].off ? vb->size - s.vbs[v].off : 0;
+            note_read(use, vb->mem);
+          }
+        if(k == Pkt::DrawIndexed && s.ib && s.ib->mem)
+        {
+          d.ib = (u64)dev_addr(s.ib->mem, s.ib->offset + s.ib_off);
+          uint32_t isz = s.ib_type == VK_INDEX_TYPE_UINT16 ? 2 : 4;
+          d.ib_count = s.ib->size > s.ib_off ? (s.ib->size - s.ib_off) / isz : 0;
+          d.index_type = s.ib_type == VK_INDEX_TYPE_UINT16 ? VGX_INDEX_U16 : VGX_INDEX_U32;
+          note_read(use, s.ib->mem);
+        }
+        else
+        {
+          d.index_type = VGX_INDEX_NONE;
+        }
+        d.first = b.first;
+        d.topology = p->topology == 4 ? VGX_TOPO_STRIP : VGX_TOPO_LIST;
+        d.num_tris = d.topology == VGX_TOPO_STRIP ? (b.count >= 3 ? b.count - 2 : 0) : b.count / 3;
+        d.cull_mode = p->cull;
+        d.front_face = p->front;
+        d.depth_op = p->depth_op;
+        d.depth_write = p->depth_write;
+        d.blend_enable = p->blend;
+        d.src_factor = p->src;
+        d.dst_factor = p->dst;
+        d.blend_op = p->op;
+        for(int a = 0; a < VGX_MAX_ATTRS; a++)
+        {
+          d.attrs[a].format = p->attrs[a].format;
+          d.attrs[a].binding = p->attrs[a].binding;
+          d.attrs[a].offset = p->attrs[a].offset;
+          d.attrs[a].stride = p->strides[p->attrs[a].binding];
+        }
+        for(size_t t = 0; t < p->tr.textures.size() && t < VGX_MAX_TEX; t++)
+        {
+          const vst::Binding &bd = p->tr.textures[t];
+          VkDescriptorSet_T *set = bd.set < 8 ? s.sets[bd.set] : nullptr;
+          VkDescriptorSet_T::Bind *bind = nullptr;
+          if(set)
+          {
+            auto it = set->binds.find(bd.binding);
+            if(it != set->binds.end())
+              bind = &it->second;
+          }
+          fill_texture(d.tex[t], bind);
+          if(bind && bind->view && bind->view->image)
+            note_read(use, bind->view->image->mem);
+        }
+        for(size_t u = 0; u < p->tr.ubos.size() && u < VGX_MAX_UBO; u++)
+        {
+          const vst::Binding &bd = p->tr.ubos[u];
+          VkDescriptorSet_T *set = bd.set < 8 ? s.sets[bd.set] : nullptr;
+          if(!set)
+            continue;
+          auto it = set->binds.find(bd.binding);
+          if(it != set->binds.end() && it->second.buffer && it->second.buffer->mem)
+          {
+            VkBuffer_T *ub = it->second.buffer;
+            d.ubo[u] = (u64)dev_addr(ub->mem, ub->offset + it->second.offset);
+            note_read(use, ub->mem);
+          }
+        }
+        memcpy(d.push, s.push, 128);
+        if(d.num_tris)
+          vgpu_list_draw(l, p->prog, &d, &s.target);
+        break;
+      }
+      case Pkt::CopyBuf2Img:
+      {
+        pk::CopyBuf2Img b;
+        pull(&b, sizeof(b));
+        /* whole-mip, tightly packed copies only (cmd_exec.cpp:143-173) */
+        VkImage_T *img = b.dst;
+        uint32_t mip = b.region.imageSubresource.mipLevel;
+        uint32_t w = std::max(1u, img->extent.width >> mip), h = std::max(1u, img->extent.height >> mip);
+        VkDeviceSize off = subresource_offset(img, mip, b.region.imageSubresource.baseArrayLayer);
+        if(b.src->mem && img->mem)
+        {
+          vgpu_list_copy(l, dev_addr(img->mem, img->offset + off),
+                         dev_addr(b.src->mem, b.src->offset + b.region.bufferOffset),
+                         (u64)w * h * img->bpp);
+          note_read(use, b.src->mem);
+          note_write(use, img->mem);
+        }
+        break;
+      }
+      case Pkt::CopyBuf:
+      {
+        pk::CopyBuf b;
+        pull(&b, sizeof(b));
+        if(b.src->mem && b.dst->mem)
+        {
+          vgpu_list_copy(l, dev_addr(b.dst->mem, b.dst->offset + b.region.dstOffset),
+                         dev_addr(b.src->mem, b.src->offset + b.region.srcOffset), b.region.size);
+          note_read(use, b.src->mem);
+          note_write(use, b.dst->mem);
+        }
+        break;
+      }
+    }
+  }
+  for(auto &kv : use)
+  {
+    if(kv.second & 1)
+      vgpu_list_upload(l, kv.first->dptr, kv.first->hptr, kv.first->size);
+    if(kv.second & 2)
+      vgpu_list_download(l, kv.first->hptr, kv.first->dptr, kv.first->size);
+  }
+  c->list = l;
+  c->lowered = true;
+}
+}    // namespace
+
+VISOR_EXPORT VkResult vkQueueSubmit(VkQueue q, uint32_t n, const VkSubmitInfo *submits, VkFence fence)
+{
+  for(uint32_t i = 0; i < n; i++)
+    for(uint32_t c = 0; c < submits[i].commandBufferCount; c++)
+    {
+      VkCommandBuffer cb = submits[i].pCommandBuffers[c];
+      if(!cb->lowered)
+        lower(cb);
+      int rc = vgpu_submit(q->q, cb->list);
+      if(rc)
+        return vr(rc);
+    }
+  if(fence)
+  {
+    int rc = vgpu_fence_signal(q->q, fence->f);
+    if(rc)
+      return vr(rc);
+  }
+  return VK_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------ */
+/* loader interface (icd_interface.cpp)                                     */
+/* ------------------------------------------------------------------------ */
+
+VISOR_EXPORT PFN_vkVoidFunction vkGetDeviceProcAddr(VkDevice, const char *pName);
+
+#define ICD_ENTRY(name) {#name, (PFN_vkVoidFunction)&name}
+
+namespace
+{
+struct Entry
+{
+  const char *name;
+  PFN_vkVoidFunction fn;
+};
+
+const Entry kInstanceFns[] = {
+    ICD_ENTRY(vkEnumerateInstanceExtensionProperties), ICD_ENTRY(vkEnumerateDeviceExtensionProperties),
+    ICD_ENTRY(vkGetDeviceProcAddr), ICD_ENTRY(vkCreateInstance), ICD_ENTRY(vkDestroyInstance),
+    ICD_ENTRY(vkEnumeratePhysicalDevices), ICD_ENTRY(vkCreateDevice), ICD_ENTRY(vkEnumerateInstanceVersion),
+};
+
+const Entry kPhysFns[] = {
+    ICD_ENTRY(vkGetPhysicalDeviceFeatures), ICD_ENTRY(vkGetPhysicalDeviceProperties),
+    ICD_ENTRY(vkGetPhysicalDeviceQueueFamilyProperties), ICD_ENTRY(vkGetPhysicalDeviceMemoryProperties),
+    ICD_ENTRY(vkGetPhysicalDeviceFormatProperties),
+};
+
+const Entry kDeviceFns[] = {
+    ICD_ENTRY(vkDestroyDevice), ICD_ENTRY(vkGetDeviceQueue), ICD_ENTRY(vkCreateFence), ICD_ENTRY(vkDestroyFence),
+    ICD_ENTRY(vkCreateSemaphore), ICD_ENTRY(vkDestroySemaphore), ICD_ENTRY(vkCreateCommandPool),
+    ICD_ENTRY(vkDestroyCommandPool), ICD_ENTRY(vkAllocateCommandBuffers), ICD_ENTRY(vkFreeCommandBuffers),
+    ICD_ENTRY(vkBeginCommandBuffer), ICD_ENTRY(vkEndCommandBuffer), ICD_ENTRY(vkCreateImageView),
+    ICD_ENTRY(vkDestroyImageView), ICD_ENTRY(vkCreateImage), ICD_ENTRY(vkDestroyImage), ICD_ENTRY(vkCreateBuffer),
+    ICD_ENTRY(vkDestroyBuffer), ICD_ENTRY(vkGetBufferMemoryRequirements), ICD_ENTRY(vkGetImageMemoryRequirements),
+    ICD_ENTRY(vkBindBufferMemory), ICD_ENTRY(vkBindImageMemory), ICD_ENTRY(vkAllocateMemory),
+    ICD_ENTRY(vkFreeMemory), ICD_ENTRY(vkMapMemory), ICD_ENTRY(vkUnmapMemory), ICD_ENTRY(vkFlushMappedMemoryRanges),
+    ICD_ENTRY(vkGetImageSubresourceLayout), ICD_ENTRY(vkCreateSampler), ICD_ENTRY(vkDestroySampler),
+    ICD_ENTRY(vkCreateDescriptorSetLayout), ICD_ENTRY(vkDestroyDescriptorSetLayout),
+    ICD_ENTRY(vkCreatePipelineLayout), ICD_ENTRY(vkDestroyPipelineLayout), ICD_ENTRY(vkCreateFramebuffer),
+    ICD_ENTRY(vkDestroyFramebuffer), ICD_ENTRY(vkCreateRenderPass), ICD_ENTRY(vkDestroyRenderPass),
+    ICD_ENTRY(vkCreateShaderModule), ICD_ENTRY(vkDestroyShaderModule), ICD_ENTRY(vkCreatePipelineCache),
+    ICD_ENTRY(vkDestroyPipelineCache), ICD_ENTRY(vkCreateGraphicsPipelines), ICD_ENTRY(vkCreateComputePipelines),
+    ICD_ENTRY(vkDestroyPipeline), ICD_ENTRY(vkCreateDescriptorPool), ICD_ENTRY(vkDestroyDescriptorPool),
+    ICD_ENTRY(vkAllocateDescriptorSets), ICD_ENTRY(vkFreeDescriptorSets), ICD_ENTRY(vkUpdateDescriptorSets),
+    ICD_ENTRY(vkCmdPipelineBarrier), ICD_ENTRY(vkCmdBeginRenderPass), ICD_ENTRY(vkCmdEndRenderPass),
+    ICD_ENTRY(vkCmdBindIndexBuffer), ICD_ENTRY(vkCmdBindVertexBuffers), ICD_ENTRY(vkCmdBindPipeline),
+    ICD_ENTRY(vkCmdBindDescriptorSets), ICD_ENTRY(vkCmdSetViewport), ICD_ENTRY(vkCmdSetScissor),
+    ICD_ENTRY(vkCmdPushConstants), ICD_ENTRY(vkCmdDraw), ICD_ENTRY(vkCmdDrawIndexed),
+    ICD_ENTRY(vkCmdCopyBufferToImage), ICD_ENTRY(vkCmdCopyBuffer), ICD_ENTRY(vkQueueSubmit),
+    ICD_ENTRY(vkWaitForFences), ICD_ENTRY(vkResetFences), ICD_ENTRY(vkDeviceWaitIdle), ICD_ENTRY(vkQueueWaitIdle),
+};
+
+template <size_t N>
+PFN_vkVoidFunction lookup(const Entry (&t)[N], const char *name)
+{
+  for(size_t i = 0; i < N; i++)
+    if(!strcmp(t[i].name, name))
+      return t[i].fn;
+  return nullptr;
+}
+}    // namespace
+
+VISOR_EXPORT PFN_vkVoidFunction vkGetDeviceProcAddr(VkDevice, const char *pName)
+{
+  return pName ? lookup(kDeviceFns, pName) : nullptr;
+}
+
+VISOR_EXPORT PFN_vkVoidFunction vk_icdGetInstanceProcAddr(VkInstance, const char *pName)
+{
+  if(!pName)
+    return nullptr;
+  if(PFN_vkVoidFunction f = lookup(kInstanceFns, pName))
+    return f;
+  if(PFN_vkVoidFunction f = lookup(kPhysFns, pName))
+    return f;
+  return lookup(kDeviceFns, pName);
+}
+
+VISOR_EXPORT PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance, const char *pName)
+{
+  return pName ? lookup(kPhysFns, pName) : nullptr;
+}
+
+VISOR_EXPORT VkResult vk_icdNegotiateLoaderICDInterfaceVersion(uint32_t *pSupportedVersion)
+{
+  if(!pSupportedVersion)
+    return VK_ERROR_INITIALIZATION_FAILED;
+  *pSupportedVersion = std::min<uint32_t>(CURRENT_LOADER_ICD_INTERFACE_VERSION, *pSupportedVersion);
+  return VK_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------ */
+/* project extensions                                                        */
+/* ------------------------------------------------------------------------ */
+
+VISOR_EXPORT void visor_gb300_set_mode(int mode) { g_mode = mode; }
+VISOR_EXPORT int visor_gb300_get_mode(void) { return default_mode(); }
+
+VISOR_EXPORT int visor_gb300_queue_stats(VkQueue q, vgpu_stats *out) { return vgpu_queue_stats(q->q, out); }
+
+VISOR_EXPORT void visor_gb300_queue_reset_stats(VkQueue q) { vgpu_queue_reset_stats(q->q); }
+
+VISOR_EXPORT size_t visor_gb300_pipeline_source(VkPipeline p, char *buf, size_t size)
+{
+  const std::string &s = p->tr.source;
+  if(buf && size)
+  {
+    size_t n = std::min(size - 1, s.size());
+    memcpy(buf, s.data(), n);
+    buf[n] = 0;
+  }
+  return s.size();
+}
+
+/* Translate a vertex/fragment SPIR-V pair to the CUDA source a pipeline would
+   compile (no device needed).  Returns the source length, 0 on failure with
+   the reason in err. */
+VISOR_EXPORT size_t visor_gb300_translate(const uint32_t *vs_words, size_t vs_count,
+                                          const uint32_t *fs_words, size_t fs_count, char *out,
+                                          size_t size, char *err, size_t err_size)
+{
+  std::string e;
+  vst::Module *vs = vst::parse(vs_words, vs_count, e);
+  vst::Module *fs = vs ? vst::parse(fs_words, fs_count, e) : nullptr;
+  vst::Result r;
+  bool ok = vs && fs && vst::translate(vs, "main", fs, "main", r, e);
+  vst::destroy(vs);
+  vst::destroy(fs);
+  if(!ok)
+  {
+    if(err && err_size)
+      snprintf(err, err_size, "%s", e.c_str());
+    return 0;
+  }
+  if(out && size)
+  {
+    size_t n = std::min(size - 1, r.source.size());
+    memcpy(out, r.source.data(), n);
+    out[n] = 0;
+  }
+  return r.source.size();
+}

@@ -1,0 +1,543 @@
+/*
+ * vgx_stage.cuh - the pipeline-specific stage kernels of the draw path.
+ *
+ * NVRTC compiles this file at vkCreateGraphicsPipelines time, after the
+ * translated shaders, which define:
+ *   VGX_K          interpolated float slots the fragment shader reads
+ *   VGX_LOD_SLOT   slot of the sampled uv (-1: none) used for the trilinear LOD
+ *   VGX_LOD_TEX    texture slot whose size scales that LOD
+ *   vgx_vs(D, vertex_index, pos, out[VGX_K])
+ *   vgx_fs(D, bary[4], i0, i1, i2, lod) -> float4
+ *
+ * vgx_setup  one thread per triangle: index fetch, 3 vertex-shader calls
+ *            (ShadeVerts, rasterizer.cpp:121-237), ToWindow (:239-253), area,
+ *            cull and bbox (:385-452), the setup record, and the number of
+ *            screen tiles the triangle touches.
+ * vgx_raster one warp per 8x8 tile, persistent over a tile queue.  Each lane
+ *            owns two pixels whose colour and depth stay in registers for the
+ *            whole tile.  Triangles arrive in primitive order in batches of 32:
+ *            coverage words per pixel (integer edge functions, :282-310 and
+ *            :538-549), ordered early depth test (:551-577), the fragment
+ *            shader on the compacted list of passing fragments, then blending
+ *            and the BGRA8/D32 writes in primitive order per pixel (:580-683).
+ */
+#ifndef VGX_STAGE_CUH
+#define VGX_STAGE_CUH
+
+#ifndef VGX_TILE_SHIFT
+#define VGX_TILE_SHIFT 3
+#endif
+#define VGX_TILE (1 << VGX_TILE_SHIFT)
+#define VGX_REC (((VGX_REC_HEAD + 3 * VGX_K) + 3) & ~3)
+/* 8 warps per CTA while the per-warp record batch fits static shared memory */
+#define VGX_RASTER_WARPS (VGX_REC > 40 ? 4 : 8)
+
+/* state word */
+#define S_DEPTH_OP(s) ((s)&7u)
+#define S_DEPTH_WRITE 8u
+#define S_BLEND 16u
+#define S_SRC(s) (((s) >> 5) & 31u)
+#define S_DST(s) (((s) >> 10) & 31u)
+#define S_DEPTH_TEST 32768u
+#define S_BLEND_OP(s) (((s) >> 16) & 7u)
+
+__device__ __forceinline__ u32 vgx_find_draw(const VgxDraw *draws, u32 n, u32 tri)
+{
+  u32 lo = 0, hi = n - 1;
+  while(lo < hi)
+  {
+    u32 mid = (lo + hi + 1) >> 1;
+    if(draws[mid].tri_base <= tri)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ u32 vgx_count_tiles(const int *r)
+{
+  return vgx_visit_tiles(r, VGX_TILE_SHIFT, [](u32, int, int) {});
+}
+
+__device__ __forceinline__ void vgx_warp_add_u64(u64 *dst, u64 v)
+{
+  unsigned long long s = v;
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1)
+    s += __shfl_down_sync(0xffffffffu, s, o);
+  if((threadIdx.x & 31) == 0 && s)
+    atomicAdd((unsigned long long *)dst, s);
+}
+
+extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
+{
+  vgx_init_unorm8();
+  __syncthreads();
+  const u32 tri = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = tri < job.num_tris;
+  const VgxDraw *draws = (const VgxDraw *)job.draws;
+  u32 *counts = (u32 *)job.counts;
+  u32 keep = 0, tested = 0;
+  if(live)
+  {
+    const u32 di = vgx_find_draw(draws, job.num_draws, tri);
+    const VgxDraw &D = draws[di];
+    const VgxTarget T = ((const VgxTarget *)job.targets)[D.target];
+    const u32 local = tri - D.tri_base;
+    u32 vi[3];
+    if(D.topology == VGX_TOPO_STRIP)
+    {
+      /* ShadeVerts strip order (rasterizer.cpp:150-232): odd triangles swap the first two */
+      vi[0] = (local & 1u) ? local + 1 : local;
+      vi[1] = (local & 1u) ? local : local + 1;
+      vi[2] = local + 2;
+    }
+    else
+    {
+      vi[0] = local * 3;
+      vi[1] = local * 3 + 1;
+      vi[2] = local * 3 + 2;
+    }
+    float4 pos[3];
+    float iv[3][VGX_K > 0 ? VGX_K : 1];
+    bool bad = false;
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+    {
+      u32 e = D.first + vi[k];
+      u32 idx = e;
+      if(D.index_type != VGX_INDEX_NONE)
+      {
+        if((u64)e >= D.ib_count)
+        {
+          bad = true;
+          idx = 0;
+        }
+        else
+        {
+          idx = D.index_type == VGX_INDEX_U16 ? (u32)__ldg((const u16 *)D.ib + e)
+                                              : __ldg((const u32 *)D.ib + e);
+        }
+      }
+      vgx_vs(D, idx, pos[k], iv[k]);
+    }
+    if(bad)
+      atomicOr((u32 *)job.status, VGX_STATUS_BAD_INDEX);
+
+    int wx[3], wy[3];
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+    {
+      /* ToWindow: truncation, no sub-pixel bits */
+      wx[k] = (int)((pos[k].x / pos[k].w + 1.0f) * 0.5f * (float)T.width);
+      wy[k] = (int)((pos[k].y * -1.0f / pos[k].w + 1.0f) * 0.5f * (float)T.height);
+    }
+    int area2 = (wx[1] - wx[0]) * (wy[2] - wy[0]) - (wy[1] - wy[0]) * (wx[2] - wx[0]);
+    u32 ntiles = 0;
+    if(area2 != 0 && !bad)
+    {
+      int area2_flipped = area2, barymul = 1;
+      if(D.front_face == 1u)
+      {
+        barymul = -barymul;
+        area2_flipped = -area2_flipped;
+      }
+      bool culled = false;
+      if(area2_flipped > 0 && (D.cull_mode & 1u))
+        culled = true;
+      if(area2_flipped < 0)
+      {
+        if(D.cull_mode & 2u)
+          culled = true;
+        barymul = -barymul;
+        area2_flipped = -area2_flipped;
+      }
+      if(!culled)
+      {
+        keep = 1;
+        int minx = min(min(wx[0], wx[1]), wx[2]), maxx = max(max(wx[0], wx[1]), wx[2]);
+        int miny = min(min(wy[0], wy[1]), wy[2]), maxy = max(max(wy[0], wy[1]), wy[2]);
+        minx = max(0, minx);
+        miny = max(0, miny);
+        maxx = min(T.width - 1, maxx);
+        maxy = min(T.height - 1, maxy);
+        if(maxx > minx && maxy > miny)
+        {
+          tested = (u32)(maxx - minx) * (u32)(maxy - miny);
+          int r[VGX_REC_HEAD];
+          r[R_V0X] = wx[0];
+          r[R_V0Y] = wy[0];
+          r[R_ABX] = wx[1] - wx[0];
+          r[R_ABY] = wy[1] - wy[0];
+          r[R_ACX] = wx[2] - wx[0];
+          r[R_ACY] = wy[2] - wy[0];
+          r[R_AREA2] = area2;
+          r[R_BARYMUL] = barymul;
+          r[R_MIN] = (int)((u32)minx | ((u32)miny << 16));
+          r[R_MAX] = (int)((u32)maxx | ((u32)maxy << 16));
+          float invarea = 1.0f / (float)area2_flipped;
+          r[R_INVAREA] = __float_as_int(invarea);
+#pragma unroll
+          for(int k = 0; k < 3; k++)
+          {
+            float invw = 1.0f / pos[k].w;
+            r[R_INVW + k] = __float_as_int(invw);
+            r[R_DEPTH + k] = __float_as_int(pos[k].z * invw);
+          }
+          r[R_DRAW] = (int)di;
+          float lod = 0.0f;
+#if VGX_LOD_SLOT >= 0
+          {
+            const VgxTex &tx = D.tex[VGX_LOD_TEX];
+            if(tx.base && tx.filter == VGX_FILTER_TRILINEAR)
+              lod = vgx_lod(iv[0][VGX_LOD_SLOT], iv[0][VGX_LOD_SLOT + 1], iv[1][VGX_LOD_SLOT],
+                            iv[1][VGX_LOD_SLOT + 1], iv[2][VGX_LOD_SLOT], iv[2][VGX_LOD_SLOT + 1],
+                            tx.width, tx.height, area2);
+          }
+#endif
+          r[R_LOD] = __float_as_int(lod);
+          const bool depth_test = D.depth_op != 7u && T.depth != 0;
+          u32 st = (D.depth_op & 7u) | (depth_test && D.depth_write ? S_DEPTH_WRITE : 0u) |
+                   (D.blend_enable ? S_BLEND : 0u) | ((D.src_factor & 31u) << 5) |
+                   ((D.dst_factor & 31u) << 10) | (depth_test ? S_DEPTH_TEST : 0u) |
+                   ((D.blend_op & 7u) << 16);
+          r[R_STATE] = (int)st;
+          u32 *rec = (u32 *)job.records + (u64)tri * VGX_REC;
+#pragma unroll
+          for(int w = 0; w < VGX_REC_HEAD; w += 4)
+            *(uint4 *)(rec + w) = make_uint4(r[w], r[w + 1], r[w + 2], r[w + 3]);
+#pragma unroll
+          for(int k = 0; k < 3; k++)
+#pragma unroll
+            for(int j = 0; j < VGX_K; j++)
+              rec[VGX_REC_HEAD + k * VGX_K + j] = __float_as_uint(iv[k][j]);
+          ntiles = vgx_count_tiles(r);
+        }
+      }
+    }
+    counts[tri] = ntiles;
+  }
+  u64 *cnt = (u64 *)job.counters;
+  u32 kb = __ballot_sync(0xffffffffu, keep);
+  if((threadIdx.x & 31) == 0 && kb)
+    atomicAdd((unsigned long long *)&cnt[0], (unsigned long long)__popc(kb));
+  vgx_warp_add_u64(&cnt[1], tested);
+}
+
+/* Depth compare of ProcessTriangles (rasterizer.cpp:562-576). */
+__device__ __forceinline__ bool vgx_depth_pass(u32 op, float z, float cur)
+{
+  switch(op)
+  {
+    case 0: return false;
+    case 1: return z < cur;
+    case 2: return z == cur;
+    case 3: return z <= cur;
+    case 4: return z > cur;
+    case 5: return z != cur;
+    case 6: return z >= cur;
+    default: return true;
+  }
+}
+
+__device__ __forceinline__ float vgx_factor(u32 f, float a)
+{
+  switch(f)
+  {
+    case 0: return 0.0f;
+    case 1: return 1.0f;
+    case 6: return a;
+    case 7: return 1.0f - a;
+    default: return 1.0f; /* the reference keeps its 1.0f default for other factors */
+  }
+}
+
+__device__ __forceinline__ float vgx_clamp01(float in) { return in > 1.0f ? 1.0f : (in < 0.0f ? 0.0f : in); }
+
+/* Blend (rasterizer.cpp:593-672) and the BGRA8 write (:674-676); alpha byte kept. */
+__device__ __forceinline__ u32 vgx_blend_write(u32 st, float4 c, u32 dst)
+{
+  if(st & S_BLEND)
+  {
+    float ex = vgx_unorm8[(dst >> 16) & 0xffu];
+    float ey = vgx_unorm8[(dst >> 8) & 0xffu];
+    float ez = vgx_unorm8[dst & 0xffu];
+    float sf = vgx_factor(S_SRC(st), c.w), df = vgx_factor(S_DST(st), c.w);
+    switch(S_BLEND_OP(st))
+    {
+      case 1: c.x = sf * c.x - df * ex; c.y = sf * c.y - df * ey; c.z = sf * c.z - df * ez; break;
+      case 2: c.x = df * ex - sf * c.x; c.y = df * ey - sf * c.y; c.z = df * ez - sf * c.z; break;
+      case 3: c.x = fminf(c.x, ex); c.y = fminf(c.y, ey); c.z = fminf(c.z, ez); break;
+      case 4: c.x = fmaxf(c.x, ex); c.y = fmaxf(c.y, ey); c.z = fmaxf(c.z, ez); break;
+      default: c.x = sf * c.x + df * ex; c.y = sf * c.y + df * ey; c.z = sf * c.z + df * ez; break;
+    }
+  }
+  u32 r = (u32)(u8)(vgx_clamp01(c.x) * 255.0f);
+  u32 g = (u32)(u8)(vgx_clamp01(c.y) * 255.0f);
+  u32 b = (u32)(u8)(vgx_clamp01(c.z) * 255.0f);
+  return (dst & 0xff000000u) | (r << 16) | (g << 8) | b;
+}
+
+/* Integer barycentrics of pixel (x,y) for a record (barycentric, rasterizer.cpp:282-310). */
+__device__ __forceinline__ void vgx_bary(const u32 *r, int x, int y, int &b0, int &b1, int &b2)
+{
+  const int PAx = (int)r[R_V0X] - x;
+  const int PAy = (int)r[R_V0Y] - y;
+  const int ux = ((int)r[R_ACX] * PAy) - ((int)r[R_ACY] * PAx);
+  const int uy = (PAx * (int)r[R_ABY]) - (PAy * (int)r[R_ABX]);
+  const int bm = (int)r[R_BARYMUL];
+  b0 = ((int)r[R_AREA2] - (ux + uy)) * bm;
+  b1 = ux * bm;
+  b2 = uy * bm;
+}
+
+__device__ __forceinline__ bool vgx_covers(const u32 *r, int x, int y)
+{
+  u32 mn = r[R_MIN], mx = r[R_MAX];
+  if(x < (int)(mn & 0xffffu) || x >= (int)(mx & 0xffffu) || y < (int)(mn >> 16) ||
+     y >= (int)(mx >> 16))
+    return false;
+  int b0, b1, b2;
+  vgx_bary(r, x, y, b0, b1, b2);
+  return (b0 | b1 | b2) >= 0;
+}
+
+__device__ __forceinline__ float vgx_pixdepth(const u32 *r, int b0, int b1, int b2, float *n)
+{
+  const float invarea = __uint_as_float(r[R_INVAREA]);
+  n[0] = (float)b0 * invarea;
+  n[1] = (float)b1 * invarea;
+  n[2] = (float)b2 * invarea;
+  return n[0] * __uint_as_float(r[R_DEPTH]) + n[1] * __uint_as_float(r[R_DEPTH + 1]) +
+         n[2] * __uint_as_float(r[R_DEPTH + 2]);
+}
+
+extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(VgxJob job)
+{
+  __shared__ __align__(16) u32 s_rec[VGX_RASTER_WARPS][32][VGX_REC];
+  __shared__ float4 s_col[VGX_RASTER_WARPS][32];
+  __shared__ u32 s_pass[VGX_RASTER_WARPS][32][2];
+  __shared__ u32 s_off[VGX_RASTER_WARPS][32];
+  vgx_init_unorm8();
+  __syncthreads();
+
+  u32 *status = (u32 *)job.status;
+  if(status[0] & VGX_STATUS_PAIR_OVERFLOW)
+    return;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const VgxDraw *draws = (const VgxDraw *)job.draws;
+  const VgxTarget *targets = (const VgxTarget *)job.targets;
+  const u32 *vals = (const u32 *)job.vals;
+  const u32 *tstart = (const u32 *)job.tile_start, *tend = (const u32 *)job.tile_end;
+  const u32 nwork = job.all_tiles ? job.num_tiles : status[3];
+  u32(*rec)[VGX_REC] = s_rec[wib];
+  u64 covered_total = 0, shaded_total = 0;
+
+  for(;;)
+  {
+    u32 w = 0;
+    if(lane == 0)
+      w = atomicAdd(&status[2], 1u);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if(w >= nwork)
+      break;
+    const u32 tile = job.work ? ((const u32 *)job.work)[w] : w;
+
+    /* target of this tile */
+    u32 lo = 0, hi = job.num_targets - 1;
+    while(lo < hi)
+    {
+      u32 mid = (lo + hi + 1) >> 1;
+      if(targets[mid].tile_base <= tile)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const VgxTarget T = targets[lo];
+    const u32 local = tile - T.tile_base;
+    const int tx = (int)(local % T.tiles_x), ty = (int)(local / T.tiles_x);
+    const int px = (tx << VGX_TILE_SHIFT) + (lane & (VGX_TILE - 1));
+    int py[2];
+    py[0] = (ty << VGX_TILE_SHIFT) + (lane >> VGX_TILE_SHIFT);
+    py[1] = py[0] + (32 >> VGX_TILE_SHIFT);
+    bool in[2];
+    u32 col[2];
+    float dep[2];
+    u32 *cbuf = (u32 *)T.color;
+    float *dbuf = (float *)T.depth;
+#pragma unroll
+    for(int p = 0; p < 2; p++)
+    {
+      in[p] = px < T.width && py[p] < T.height;
+      u64 pix = (u64)py[p] * (u32)T.width + (u32)px;
+      if(T.init_clear)
+      {
+        col[p] = T.clear_bgra;
+        dep[p] = T.clear_depth;
+      }
+      else
+      {
+        col[p] = in[p] ? cbuf[pix] : 0u;
+        dep[p] = (in[p] && dbuf) ? dbuf[pix] : 1.0f;
+      }
+    }
+
+    const u32 start = tstart[tile], end = tend[tile];
+    for(u32 base = start; base < end; base += 32)
+    {
+      const u32 n = min(32u, end - base);
+      if((u32)lane < n)
+      {
+        const u32 t = vals[base + lane];
+        const uint4 *src = (const uint4 *)((const u32 *)job.records + (u64)t * VGX_REC);
+        uint4 *dst = (uint4 *)rec[lane];
+#pragma unroll
+        for(int q = 0; q < VGX_REC / 4; q++)
+          dst[q] = __ldg(src + q);
+      }
+      __syncwarp();
+
+      /* coverage words: bit t set when triangle t of the batch covers the pixel */
+      u32 cov[2] = {0u, 0u};
+      for(u32 t = 0; t < n; t++)
+      {
+#pragma unroll
+        for(int p = 0; p < 2; p++)
+          if(in[p] && vgx_covers(rec[t], px, py[p]))
+            cov[p] |= 1u << t;
+      }
+
+      /* early depth test in primitive order per pixel */
+      u32 pass[2] = {0u, 0u};
+#pragma unroll
+      for(int p = 0; p < 2; p++)
+      {
+        u32 m = cov[p];
+        while(m)
+        {
+          const u32 t = __ffs(m) - 1;
+          m &= m - 1;
+          const u32 *r = rec[t];
+          const u32 st = r[R_STATE];
+          int b0, b1, b2;
+          vgx_bary(r, px, py[p], b0, b1, b2);
+          float nn[3];
+          const float z = vgx_pixdepth(r, b0, b1, b2, nn);
+          bool ok = true;
+          if(st & S_DEPTH_TEST)
+            ok = vgx_depth_pass(S_DEPTH_OP(st), z, dep[p]);
+          if(ok)
+          {
+            pass[p] |= 1u << t;
+            if(st & S_DEPTH_WRITE)
+              dep[p] = z;
+          }
+        }
+      }
+      covered_total += __popc(cov[0]) + __popc(cov[1]);
+      const u32 mine = __popc(pass[0]) + __popc(pass[1]);
+      shaded_total += mine;
+
+      /* compact the passing fragments across the warp */
+      u32 incl = mine;
+#pragma unroll
+      for(int o = 1; o < 32; o <<= 1)
+      {
+        u32 v = __shfl_up_sync(0xffffffffu, incl, o);
+        if(lane >= o)
+          incl += v;
+      }
+      const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+      const u32 excl = incl - mine;
+      s_off[wib][lane] = excl;
+      s_pass[wib][lane][0] = pass[0];
+      s_pass[wib][lane][1] = pass[1];
+      __syncwarp();
+
+      for(u32 chunk = 0; chunk < total; chunk += 32)
+      {
+        const u32 f = chunk + lane;
+        if(f < total)
+        {
+          /* owner lane: last lane whose exclusive offset <= f */
+          u32 olo = 0, ohi = 31;
+          while(olo < ohi)
+          {
+            u32 mid = (olo + ohi + 1) >> 1;
+            if(s_off[wib][mid] <= f)
+              olo = mid;
+            else
+              ohi = mid - 1;
+          }
+          u32 k = f - s_off[wib][olo];
+          const u32 p0 = s_pass[wib][olo][0];
+          const u32 c0 = __popc(p0);
+          const int sel = k < c0 ? 0 : 1;
+          u32 m = sel ? s_pass[wib][olo][1] : p0;
+          u32 kk = sel ? k - c0 : k;
+          while(kk--)
+            m &= m - 1;
+          const u32 t = __ffs(m) - 1;
+          const int fx = (int)(olo & (VGX_TILE - 1)) + (tx << VGX_TILE_SHIFT);
+          const int fy = (ty << VGX_TILE_SHIFT) + (int)(olo >> VGX_TILE_SHIFT) + sel * (32 >> VGX_TILE_SHIFT);
+          const u32 *r = rec[t];
+          int b0, b1, b2;
+          vgx_bary(r, fx, fy, b0, b1, b2);
+          float nb[4];
+          (void)vgx_pixdepth(r, b0, b1, b2, nb);
+          /* perspective correction, rasterizer.cpp:580-588 */
+          nb[0] = nb[0] * __uint_as_float(r[R_INVW]);
+          nb[1] = nb[1] * __uint_as_float(r[R_INVW + 1]);
+          nb[2] = nb[2] * __uint_as_float(r[R_INVW + 2]);
+          const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
+          nb[0] = nb[0] * invlen;
+          nb[1] = nb[1] * invlen;
+          nb[2] = nb[2] * invlen;
+          nb[3] = 0.0f;
+          const float *iv = (const float *)(r + VGX_REC_HEAD);
+          s_col[wib][lane] = vgx_fs(draws[r[R_DRAW]], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
+                                    __uint_as_float(r[R_LOD]));
+        }
+        __syncwarp();
+        /* in-order blend: each owner consumes its fragments of this chunk */
+        const u32 lo_f = max(excl, chunk), hi_f = min(excl + mine, chunk + 32);
+        for(u32 g = lo_f; g < hi_f; g++)
+        {
+          u32 k = g - excl;
+          const u32 c0 = __popc(pass[0]);
+          const int sel = k < c0 ? 0 : 1;
+          u32 m = sel ? pass[1] : pass[0];
+          u32 kk = sel ? k - c0 : k;
+          while(kk--)
+            m &= m - 1;
+          const u32 t = __ffs(m) - 1;
+          const float4 c = s_col[wib][g - chunk];
+          const u32 st = rec[t][R_STATE];
+          if(sel == 0)
+            col[0] = vgx_blend_write(st, c, col[0]);
+          else
+            col[1] = vgx_blend_write(st, c, col[1]);
+        }
+        __syncwarp();
+      }
+    }
+
+#pragma unroll
+    for(int p = 0; p < 2; p++)
+    {
+      if(in[p])
+      {
+        u64 pix = (u64)py[p] * (u32)T.width + (u32)px;
+        cbuf[pix] = col[p];
+        if(dbuf)
+          dbuf[pix] = dep[p];
+      }
+    }
+  }
+  u64 *cnt = (u64 *)job.counters;
+  vgx_warp_add_u64(&cnt[2], covered_total);
+  vgx_warp_add_u64(&cnt[3], shaded_total);
+}
+
+#endif

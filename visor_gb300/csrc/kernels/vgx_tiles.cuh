@@ -1,0 +1,84 @@
+/*
+ * vgx_tiles.cuh - which screen tiles a triangle touches.
+ *
+ * Used by the setup kernel (to count) and by the binning kernel (to emit the
+ * (tile, triangle) pairs); both must enumerate exactly the same tiles in the
+ * same order, so the enumeration lives here once.
+ */
+#ifndef VGX_TILES_CUH
+#define VGX_TILES_CUH
+
+/* record words shared by setup, binning and raster */
+#define R_V0X 0
+#define R_V0Y 1
+#define R_ABX 2
+#define R_ABY 3
+#define R_ACX 4
+#define R_ACY 5
+#define R_AREA2 6
+#define R_BARYMUL 7
+#define R_MIN 8
+#define R_MAX 9
+#define R_INVAREA 10
+#define R_DEPTH 11
+#define R_INVW 14
+#define R_DRAW 17
+#define R_LOD 18
+#define R_STATE 19
+#define VGX_REC_HEAD 20
+
+/* Conservative tile test: a tile can hold covered pixels only if every
+   (barymul-signed) edge function is >= 0 at some corner of its pixel rectangle
+   [x0,x1]x[y0,y1] (inclusive).  The functions are affine, so their maxima lie
+   on corners; evaluation uses the integer arithmetic of the per-pixel test
+   (rasterizer.cpp:303-309), so no covered pixel is ever dropped. */
+__device__ __forceinline__ bool vgx_tile_touched(const int *r, int x0, int y0, int x1, int y1)
+{
+  const int v0x = r[R_V0X], v0y = r[R_V0Y], ABx = r[R_ABX], ABy = r[R_ABY], ACx = r[R_ACX],
+            ACy = r[R_ACY], area2 = r[R_AREA2], bm = r[R_BARYMUL];
+  int m0 = -2147483647 - 1, m1 = m0, m2 = m0;
+#pragma unroll
+  for(int c = 0; c < 4; c++)
+  {
+    const int x = (c & 1) ? x1 : x0, y = (c & 2) ? y1 : y0;
+    const int PAx = v0x - x, PAy = v0y - y;
+    const int ux = (ACx * PAy) - (ACy * PAx);
+    const int uy = (PAx * ABy) - (PAy * ABx);
+    m0 = max(m0, (area2 - (ux + uy)) * bm);
+    m1 = max(m1, ux * bm);
+    m2 = max(m2, uy * bm);
+  }
+  return m0 >= 0 && m1 >= 0 && m2 >= 0;
+}
+
+/* Visit, in row-major order, every tile of edge 2^shift the record's pixel
+   rectangle [minx,maxx) x [miny,maxy) touches. */
+template <typename F>
+__device__ __forceinline__ u32 vgx_visit_tiles(const int *r, u32 shift, F fn)
+{
+  const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
+  const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
+  const int tx0 = minx >> shift, tx1 = (maxx - 1) >> shift;
+  const int ty0 = miny >> shift, ty1 = (maxy - 1) >> shift;
+  const bool small = (tx1 - tx0 + 1) * (ty1 - ty0 + 1) <= 2;
+  u32 c = 0;
+  for(int ty = ty0; ty <= ty1; ty++)
+    for(int tx = tx0; tx <= tx1; tx++)
+    {
+      bool hit = small;
+      if(!small)
+      {
+        const int x0 = max(minx, tx << shift), x1 = min(maxx, (tx + 1) << shift) - 1;
+        const int y0 = max(miny, ty << shift), y1 = min(maxy, (ty + 1) << shift) - 1;
+        hit = vgx_tile_touched(r, x0, y0, x1, y1);
+      }
+      if(hit)
+      {
+        fn(c, tx, ty);
+        c++;
+      }
+    }
+  return c;
+}
+
+#endif

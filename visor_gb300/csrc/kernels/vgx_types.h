@@ -1,0 +1,128 @@
+/*
+ * vgx_types.h - device-visible data layout of the draw path.
+ *
+ * Shared verbatim by the host runtime (C++/nvcc) and by the stage kernels that
+ * NVRTC compiles at pipeline creation, so every structure is plain data with
+ * fixed-width fields.  One "job" is a run of draws that share a shader pair;
+ * its triangles are numbered in primitive order across draws (draw order, then
+ * triangle order within the draw), which is the order every pixel must see
+ * them in (rasterizer.cpp:488-515 in serial FIFO mode).
+ *
+ * HBM layout of a job:
+ *   draws      VgxDraw[num_draws]          per-draw state, push constants, bindings
+ *   targets    VgxTarget[num_targets]      framebuffers (BGRA8 colour, D32 depth)
+ *   records    u32[num_tris * VGX_REC]     triangle setup records (setup -> raster)
+ *   counts     u32[num_tris + 1]           tiles touched per triangle, then scanned
+ *   keys/vals  u32[pair_capacity] x2 x2    (tile, triangle) pairs + sort ping-pong
+ *   tile_start/tile_end u32[num_tiles]     per-tile slice of the sorted pairs
+ */
+#ifndef VGX_TYPES_H
+#define VGX_TYPES_H
+
+#ifdef __CUDACC_RTC__
+typedef unsigned int u32;
+typedef int i32;
+typedef unsigned long long u64;
+typedef unsigned char u8;
+typedef unsigned short u16;
+#else
+#include <stdint.h>
+typedef uint32_t u32;
+typedef int32_t i32;
+typedef uint64_t u64;
+typedef uint8_t u8;
+typedef uint16_t u16;
+#endif
+
+#define VGX_MAX_ATTRS 8
+#define VGX_MAX_VB 4
+#define VGX_MAX_TEX 4
+#define VGX_MAX_UBO 4
+#define VGX_MAX_MIPS 15
+
+/* vertex attribute formats (VkFormat values the fetch understands) */
+#define VGX_FMT_NONE 0u
+#define VGX_FMT_RGBA8_UNORM 37u
+#define VGX_FMT_R32 100u
+#define VGX_FMT_RG32 103u
+#define VGX_FMT_RGB32 106u
+#define VGX_FMT_RGBA32 109u
+
+#define VGX_FILTER_REFERENCE 0u
+#define VGX_FILTER_TRILINEAR 1u
+#define VGX_FILTER_NEAREST 2u
+
+#define VGX_INDEX_U16 0u
+#define VGX_INDEX_U32 1u
+#define VGX_INDEX_NONE 2u
+
+#define VGX_TOPO_LIST 3u
+#define VGX_TOPO_STRIP 4u
+
+/* status word bits (VgxJob::status[0]) */
+#define VGX_STATUS_PAIR_OVERFLOW 1u
+#define VGX_STATUS_BAD_INDEX 2u
+
+typedef struct VgxAttr {
+  u32 format; /* VGX_FMT_* ; NONE -> (0,0,0,1) */
+  u32 binding;
+  u32 offset;
+  u32 stride;
+} VgxAttr;
+
+typedef struct VgxTex {
+  u64 base; /* device address of mip 0 */
+  u32 width, height, mips, filter;
+  u32 mip_offset[VGX_MAX_MIPS + 1]; /* byte offset of each mip from base (tight packing) */
+} VgxTex;
+
+typedef struct VgxDraw {
+  u64 vb[VGX_MAX_VB]; /* device address of each bound vertex buffer (+ bind offset) */
+  u64 vb_bytes[VGX_MAX_VB]; /* bytes readable from vb[i] (bounds for the fetch) */
+  u64 ib;         /* device address of the index buffer (+ bind offset) */
+  u64 ib_count;   /* indices readable from ib */
+  u32 index_type; /* VGX_INDEX_* */
+  u32 first;      /* firstIndex or firstVertex */
+  u32 tri_base;   /* first job-triangle id of this draw */
+  u32 num_tris;
+  u32 topology;
+  u32 target;
+  u32 cull_mode, front_face, depth_op, depth_write;
+  u32 blend_enable, src_factor, dst_factor, blend_op;
+  VgxAttr attrs[VGX_MAX_ATTRS]; /* indexed by location */
+  u64 ubo[VGX_MAX_UBO];         /* uniform buffer slots resolved at pipeline creation */
+  VgxTex tex[VGX_MAX_TEX];      /* sampled image slots resolved at pipeline creation */
+  u8 push[128];
+} VgxDraw;
+
+typedef struct VgxTarget {
+  u64 color;      /* BGRA8, width*height*4 bytes */
+  u64 depth;      /* f32, width*height; 0 when the subpass has no depth attachment */
+  i32 width, height;
+  u32 tiles_x, tiles_y;
+  u32 tile_base;  /* first job-tile id of this target */
+  u32 init_clear; /* 1: tiles start from the clear values instead of memory */
+  u32 clear_bgra; /* clear colour as stored bytes (B,G,R,A little-endian) */
+  float clear_depth;
+} VgxTarget;
+
+typedef struct VgxJob {
+  u64 draws;   /* VgxDraw* */
+  u64 targets; /* VgxTarget* */
+  u64 records; /* u32* */
+  u64 counts;  /* u32*, num_tris + 1 */
+  u64 keys, vals, keys_alt, vals_alt; /* u32* pair arrays */
+  u64 tile_start, tile_end;           /* u32* per tile */
+  u64 work;                           /* u32* tiles to raster; 0 = every tile in order */
+  u64 status;                         /* u32*: [0] flags, [1] pair total, [2] work queue, [3] work count */
+  u64 counters;                       /* u64*: tris_out, tested, covered, shaded */
+  u64 scratch;                        /* u32* scan/sort scratch */
+  u32 num_draws, num_tris;
+  u32 num_targets, num_tiles;
+  u32 pair_capacity;
+  u32 tile_shift; /* log2 of the tile edge in pixels */
+  u32 key_bits;   /* bits needed for a tile id */
+  u32 all_tiles;  /* 1: raster every tile (fused clear), 0: only tiles with triangles */
+} VgxJob;
+
+#endif

@@ -1,0 +1,1357 @@
+/*
+ * vgpu.cu - CUDA back end of the draw path (see include/visor_gpu.h).
+ *
+ * Replaces the reference's CPU rasterizer driver loop: DrawTriangles
+ * (rasterizer.cpp:363-520) with its 32x32 block queue and thread pool becomes
+ *
+ *   setup   (NVRTC, per pipeline)  VS x3 + setup record + tiles touched
+ *   scan    exclusive scan of the per-triangle tile counts
+ *   emit    (tile, triangle) pairs in triangle order
+ *   sort    stable LSD radix sort of the pairs by tile id (primitive order kept)
+ *   ranges  per-tile slice of the sorted pairs (+ the list of non-empty tiles)
+ *   raster  (NVRTC, per pipeline)  warp per tile, primitive-ordered ROP
+ *
+ * A list is split into segments at copies.  Within a segment every job's
+ * setup and scan run first (they read only geometry), one synchronisation
+ * reads the pair totals so pair storage can grow, then clears, binning and
+ * raster run in command order.  Batched lists merge consecutive draws that
+ * share a pipeline into one job across render targets and fuse render-pass
+ * clears into the raster; per-draw lists launch the whole chain per draw.
+ */
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <time.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "visor_gpu.h"
+#include "../kernels/vgx_tiles.cuh"
+
+#include "vgx_sources.inc" /* generated: kVgxTypes, kVgxDevice, kVgxTiles, kVgxStage */
+
+#define CK(x)                                                                               \
+  do                                                                                        \
+  {                                                                                         \
+    cudaError_t e_ = (x);                                                                   \
+    if(e_ != cudaSuccess)                                                                   \
+    {                                                                                       \
+      fprintf(stderr, "visor_gb300: %s failed: %s (%s:%d)\n", #x, cudaGetErrorString(e_),    \
+              __FILE__, __LINE__);                                                          \
+      return e_ == cudaErrorMemoryAllocation ? VGPU_ERROR_OUT_OF_DEVICE_MEMORY              \
+                                             : VGPU_ERROR_DEVICE_LOST;                      \
+    }                                                                                       \
+  } while(0)
+
+/* Driver-API entry points, resolved through the runtime so the library loads on
+   hosts without a GPU driver (the build and CPU tests only need the symbols). */
+struct DriverApi
+{
+  CUresult (*moduleLoadData)(CUmodule *, const void *) = nullptr;
+  CUresult (*moduleGetFunction)(CUfunction *, CUmodule, const char *) = nullptr;
+  CUresult (*moduleUnload)(CUmodule) = nullptr;
+  CUresult (*launchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                           unsigned, CUstream, void **, void **) = nullptr;
+  CUresult (*funcSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+  CUresult (*getErrorString)(CUresult, const char **) = nullptr;
+};
+static DriverApi g_cu;
+
+#define CU(x)                                                                               \
+  do                                                                                        \
+  {                                                                                         \
+    CUresult r_ = (x);                                                                      \
+    if(r_ != CUDA_SUCCESS)                                                                  \
+    {                                                                                       \
+      const char *s_ = "?";                                                                 \
+      if(g_cu.getErrorString)                                                               \
+        g_cu.getErrorString(r_, &s_);                                                       \
+      fprintf(stderr, "visor_gb300: %s failed: %s (%s:%d)\n", #x, s_, __FILE__, __LINE__);  \
+      return VGPU_ERROR_DEVICE_LOST;                                                        \
+    }                                                                                       \
+  } while(0)
+
+static int load_driver_api()
+{
+  struct
+  {
+    const char *name;
+    void **slot;
+  } fns[] = {
+      {"cuModuleLoadData", (void **)&g_cu.moduleLoadData},
+      {"cuModuleGetFunction", (void **)&g_cu.moduleGetFunction},
+      {"cuModuleUnload", (void **)&g_cu.moduleUnload},
+      {"cuLaunchKernel", (void **)&g_cu.launchKernel},
+      {"cuFuncSetAttribute", (void **)&g_cu.funcSetAttribute},
+      {"cuGetErrorString", (void **)&g_cu.getErrorString},
+  };
+  for(auto &f : fns)
+  {
+    cudaDriverEntryPointQueryResult q;
+    if(cudaGetDriverEntryPointByVersion(f.name, f.slot, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+       q != cudaDriverEntryPointSuccess || !*f.slot)
+    {
+      fprintf(stderr, "visor_gb300: driver entry point %s unavailable\n", f.name);
+      return VGPU_ERROR_INITIALIZATION_FAILED;
+    }
+  }
+  return VGPU_OK;
+}
+
+namespace
+{
+std::mutex g_mu;
+bool g_init = false;
+int g_sms = 148;
+vgpu_tuning g_tuning = {2, 1};
+
+/* ------------------------------------------------------------------------ */
+/* generic kernels                                                           */
+/* ------------------------------------------------------------------------ */
+
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanBlock * kScanItems;
+
+__device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32 *total)
+{
+  __shared__ u32 warp_sums[kScanBlock / 32 + 1];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  u32 incl = v;
+#pragma unroll
+  for(int o = 1; o < 32; o <<= 1)
+  {
+    u32 t = __shfl_up_sync(0xffffffffu, incl, o);
+    if(lane >= o)
+      incl += t;
+  }
+  if(lane == 31)
+    warp_sums[w] = incl;
+  __syncthreads();
+  if(w == 0)
+  {
+    u32 s = lane < kScanBlock / 32 ? warp_sums[lane] : 0;
+    u32 si = s;
+#pragma unroll
+    for(int o = 1; o < 32; o <<= 1)
+    {
+      u32 t = __shfl_up_sync(0xffffffffu, si, o);
+      if(lane >= o)
+        si += t;
+    }
+    if(lane < kScanBlock / 32)
+      warp_sums[lane] = si - s;
+    if(lane == kScanBlock / 32 - 1)
+      warp_sums[kScanBlock / 32] = si; /* uses one extra slot below */
+  }
+  __syncthreads();
+  u32 res = incl - v + warp_sums[w];
+  if(total)
+    *total = warp_sums[kScanBlock / 32];
+  __syncthreads();
+  return res;
+}
+
+/* per-tile sums of `in` (kScanTile elements per block) */
+__global__ void k_scan_reduce(const u32 *in, u32 n, u32 *sums)
+{
+  __shared__ u32 s[kScanBlock / 32 + 1];
+  u32 base = blockIdx.x * kScanTile, acc = 0;
+  for(int i = 0; i < kScanItems; i++)
+  {
+    u32 idx = base + i * kScanBlock + threadIdx.x;
+    if(idx < n)
+      acc += in[idx];
+  }
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1)
+    acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if((threadIdx.x & 31) == 0)
+    s[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if(threadIdx.x == 0)
+  {
+    u32 t = 0;
+    for(int i = 0; i < kScanBlock / 32; i++)
+      t += s[i];
+    sums[blockIdx.x] = t;
+  }
+}
+
+/* exclusive scan of `in` into `out` (in-place allowed), adding block offsets;
+   out[n] receives the total when write_total is set */
+__global__ void k_scan_apply(const u32 *in, u32 *out, u32 n, const u32 *offsets, int write_total)
+{
+  __shared__ u32 carry;
+  if(threadIdx.x == 0)
+    carry = offsets ? offsets[blockIdx.x] : 0;
+  __syncthreads();
+  u32 base = blockIdx.x * kScanTile;
+  /* each thread owns kScanItems consecutive elements */
+  u32 v[kScanItems], local = 0;
+  for(int i = 0; i < kScanItems; i++)
+  {
+    u32 idx = base + threadIdx.x * kScanItems + i;
+    v[i] = idx < n ? in[idx] : 0;
+    local += v[i];
+  }
+  u32 total;
+  u32 ex = block_exclusive_scan(local, &total) + carry;
+  for(int i = 0; i < kScanItems; i++)
+  {
+    u32 idx = base + threadIdx.x * kScanItems + i;
+    if(idx < n)
+      out[idx] = ex;
+    ex += v[i];
+  }
+  if(write_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == kScanBlock - 1)
+    out[n] = ex;
+}
+
+/* (tile, triangle) pairs in triangle order */
+__global__ void k_emit(VgxJob job, u32 rec_words, const u32 *offsets)
+{
+  const u32 tri = blockIdx.x * blockDim.x + threadIdx.x;
+  if(tri >= job.num_tris)
+    return;
+  const u32 n = offsets[tri + 1] - offsets[tri];
+  if(n == 0)
+    return;
+  const u32 total = offsets[job.num_tris];
+  if(total > job.pair_capacity)
+    return;
+  const int *r = (const int *)((const u32 *)job.records + (u64)tri * rec_words);
+  int head[VGX_REC_HEAD];
+#pragma unroll
+  for(int i = 0; i < VGX_REC_HEAD; i++)
+    head[i] = r[i];
+  const VgxDraw *draws = (const VgxDraw *)job.draws;
+  const VgxTarget *targets = (const VgxTarget *)job.targets;
+  const VgxTarget &T = targets[draws[head[R_DRAW]].target];
+  u32 *keys = (u32 *)job.keys, *vals = (u32 *)job.vals;
+  const u32 off = offsets[tri];
+  vgx_visit_tiles(head, job.tile_shift, [&](u32 i, int tx, int ty) {
+    keys[off + i] = T.tile_base + (u32)ty * T.tiles_x + (u32)tx;
+    vals[off + i] = tri;
+  });
+}
+
+/* stable LSD radix sort, 8-bit digits */
+constexpr int kSortBlock = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortBlock * kSortItems;
+
+__global__ void k_radix_hist(const u32 *keys, u32 n, u32 shift, u32 *hist, u32 nblocks)
+{
+  __shared__ u32 h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  u32 base = blockIdx.x * kSortTile;
+  for(int i = 0; i < kSortItems; i++)
+  {
+    u32 idx = base + i * kSortBlock + threadIdx.x;
+    if(idx < n)
+      atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_radix_scatter(const u32 *keys, const u32 *vals, u32 n, u32 shift,
+                                const u32 *hist_scanned, u32 nblocks, u32 *okeys, u32 *ovals)
+{
+  __shared__ u32 base_d[256];
+  __shared__ u32 wcnt[kSortBlock / 32][256];
+  __shared__ u32 tot[256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  base_d[threadIdx.x] = hist_scanned[threadIdx.x * nblocks + blockIdx.x];
+  const u32 lt = (1u << lane) - 1u;
+  for(int round = 0; round < kSortItems; round++)
+  {
+    for(int k = threadIdx.x; k < (kSortBlock / 32) * 256; k += kSortBlock)
+      (&wcnt[0][0])[k] = 0;
+    __syncthreads();
+    const u32 idx = blockIdx.x * kSortTile + round * kSortBlock + threadIdx.x;
+    const bool valid = idx < n;
+    const u32 key = valid ? keys[idx] : 0u;
+    const u32 dig = (key >> shift) & 255u;
+    const u32 peers = __match_any_sync(0xffffffffu, valid ? dig : 256u + lane);
+    const u32 rank = __popc(peers & lt);
+    if(valid && rank == 0)
+      wcnt[w][dig] = __popc(peers);
+    __syncthreads();
+    {
+      u32 s = 0;
+      for(int ww = 0; ww < kSortBlock / 32; ww++)
+      {
+        u32 c = wcnt[ww][threadIdx.x];
+        wcnt[ww][threadIdx.x] = s;
+        s += c;
+      }
+      tot[threadIdx.x] = s;
+    }
+    __syncthreads();
+    if(valid)
+    {
+      const u32 pos = base_d[dig] + wcnt[w][dig] + rank;
+      okeys[pos] = key;
+      ovals[pos] = vals[idx];
+    }
+    __syncthreads();
+    base_d[threadIdx.x] += tot[threadIdx.x];
+    __syncthreads();
+  }
+}
+
+/* per-tile [start, end) of the sorted pairs, and the queue of non-empty tiles */
+__global__ void k_ranges(const u32 *keys, const u32 *pair_total, u32 capacity, u32 *tstart,
+                         u32 *tend, u32 *work, u32 *status)
+{
+  const u32 n = *pair_total;
+  if(n > capacity)
+    return;
+  for(u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    const u32 k = keys[i];
+    if(i == 0 || keys[i - 1] != k)
+    {
+      tstart[k] = i;
+      if(work)
+        work[atomicAdd(&status[3], 1u)] = k;
+    }
+    if(i == n - 1 || keys[i + 1] != k)
+      tend[k] = i + 1;
+  }
+}
+
+__global__ void k_clear(VgxTarget t, int color, int depth)
+{
+  const u64 n = (u64)t.width * (u32)t.height;
+  for(u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)
+  {
+    if(color)
+      ((u32 *)t.color)[i] = t.clear_bgra;
+    if(depth && t.depth)
+      ((float *)t.depth)[i] = t.clear_depth;
+  }
+}
+
+__global__ void k_flag_overflow(const u32 *pair_total, u32 capacity, u32 *status)
+{
+  if(*pair_total > capacity)
+    atomicOr(status, VGX_STATUS_PAIR_OVERFLOW);
+}
+
+u64 hash_str(const std::string &s)
+{
+  u64 h = 0xcbf29ce484222325ull;
+  for(unsigned char c : s)
+  {
+    h ^= c;
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+std::string cache_dir()
+{
+  const char *e = getenv("VISOR_GB300_CACHE");
+  if(e && *e)
+    return e;
+  const char *home = getenv("HOME");
+  return std::string(home ? home : "/tmp") + "/.cache/visor_gb300";
+}
+
+}    // namespace
+
+/* ------------------------------------------------------------------------ */
+/* device + memory                                                           */
+/* ------------------------------------------------------------------------ */
+
+extern "C" int vgpu_init(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if(g_init)
+    return VGPU_OK;
+  int n = 0;
+  if(cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+  {
+    fprintf(stderr, "visor_gb300: no CUDA device available\n");
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  }
+  CK(cudaSetDevice(0));
+  CK(cudaFree(0));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, 0));
+  g_sms = prop.multiProcessorCount;
+  int rc = load_driver_api();
+  if(rc)
+    return rc;
+  g_init = true;
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_device_info_get(vgpu_device_info *out)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return rc;
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, 0));
+  memset(out, 0, sizeof(*out));
+  snprintf(out->name, sizeof(out->name), "%s", prop.name);
+  out->total_memory = prop.totalGlobalMem;
+  out->sm_count = prop.multiProcessorCount;
+  out->cc_major = prop.major;
+  out->cc_minor = prop.minor;
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_mem_alloc(uint64_t bytes, int host_visible, void **dptr, void **hptr)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return rc;
+  *dptr = nullptr;
+  if(hptr)
+    *hptr = nullptr;
+  uint64_t sz = bytes ? (bytes + 255) & ~255ull : 256;
+  if(cudaMalloc(dptr, sz) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return VGPU_ERROR_OUT_OF_DEVICE_MEMORY;
+  }
+  if(host_visible)
+  {
+    if(cudaMallocHost(hptr, sz) != cudaSuccess)
+    {
+      cudaGetLastError();
+      cudaFree(*dptr);
+      *dptr = nullptr;
+      return VGPU_ERROR_OUT_OF_HOST_MEMORY;
+    }
+    memset(*hptr, 0, sz);
+  }
+  return VGPU_OK;
+}
+
+extern "C" void vgpu_mem_free(void *dptr, void *hptr)
+{
+  if(dptr)
+    cudaFree(dptr);
+  if(hptr)
+    cudaFreeHost(hptr);
+}
+
+/* ------------------------------------------------------------------------ */
+/* programs (NVRTC)                                                          */
+/* ------------------------------------------------------------------------ */
+
+struct vgpu_program
+{
+  CUmodule mod = nullptr;
+  CUfunction setup = nullptr, raster = nullptr;
+  u32 k = 0, rec_words = 0, tile_shift = 3;
+};
+
+static int compile_cubin(const std::string &src, std::vector<char> &cubin, char *log, size_t log_size)
+{
+  nvrtcProgram prog;
+  if(nvrtcCreateProgram(&prog, src.c_str(), "vgx_pipeline.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  const char *opts[] = {"--gpu-architecture=sm_103a", "--fmad=false", "--prec-div=true",
+                        "--prec-sqrt=true", "--ftz=false", "-default-device", "--std=c++17",
+                        "-lineinfo"};
+  nvrtcResult r = nvrtcCompileProgram(prog, sizeof(opts) / sizeof(opts[0]), opts);
+  size_t ls = 0;
+  nvrtcGetProgramLogSize(prog, &ls);
+  if(r != NVRTC_SUCCESS)
+  {
+    std::string l(ls, '\0');
+    nvrtcGetProgramLog(prog, &l[0]);
+    if(log && log_size)
+      snprintf(log, log_size, "%s", l.c_str());
+    fprintf(stderr, "visor_gb300: NVRTC failed:\n%.4000s\n", l.c_str());
+    nvrtcDestroyProgram(&prog);
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  cubin.resize(n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  return VGPU_OK;
+}
+
+static std::string full_source(const char *shader_source, uint32_t tile_shift)
+{
+  std::string src;
+  src += "#define VGX_TILE_SHIFT " + std::to_string(tile_shift) + "\n";
+  src += kVgxTypes;
+  src += kVgxDevice;
+  src += kVgxTiles;
+  src += shader_source;
+  src += kVgxStage;
+  return src;
+}
+
+extern "C" int vgpu_program_check(const char *shader_source, uint32_t tile_shift, char *log,
+                                  size_t log_size, uint64_t *cubin_bytes)
+{
+  std::vector<char> cubin;
+  int rc = compile_cubin(full_source(shader_source, tile_shift), cubin, log, log_size);
+  if(cubin_bytes)
+    *cubin_bytes = cubin.size();
+  return rc;
+}
+
+extern "C" int vgpu_program_create(const char *shader_source, uint32_t tile_shift,
+                                   vgpu_program **out, char *log, size_t log_size)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return rc;
+  const char *kd = strstr(shader_source, "#define VGX_K ");
+  if(!kd)
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  u32 k = (u32)atoi(kd + 14);
+  std::string src = full_source(shader_source, tile_shift);
+
+  /* compiled images are cached in memory and on disk, keyed by the full source */
+  static std::map<u64, std::vector<char>> mem_cache;
+  const u64 h = hash_str(src + "|sm_103a|fmad=false");
+  std::vector<char> cubin;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = mem_cache.find(h);
+    if(it != mem_cache.end())
+      cubin = it->second;
+  }
+  char path[1024];
+  snprintf(path, sizeof(path), "%s/%016llx.cubin", cache_dir().c_str(), (unsigned long long)h);
+  if(cubin.empty())
+  {
+    FILE *f = fopen(path, "rb");
+    if(f)
+    {
+      fseek(f, 0, SEEK_END);
+      long n = ftell(f);
+      fseek(f, 0, SEEK_SET);
+      cubin.resize(n > 0 ? n : 0);
+      if(n <= 0 || fread(cubin.data(), 1, n, f) != (size_t)n)
+        cubin.clear();
+      fclose(f);
+    }
+  }
+  if(cubin.empty())
+  {
+    rc = compile_cubin(src, cubin, log, log_size);
+    if(rc)
+      return rc;
+    std::string dir = cache_dir();
+    mkdir(dir.c_str(), 0755);
+    std::string tmp = std::string(path) + ".tmp" + std::to_string((long)getpid());
+    FILE *f = fopen(tmp.c_str(), "wb");
+    if(f)
+    {
+      fwrite(cubin.data(), 1, cubin.size(), f);
+      fclose(f);
+      rename(tmp.c_str(), path);
+    }
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    mem_cache[h] = cubin;
+  }
+  vgpu_program *p = new vgpu_program();
+  p->k = k;
+  p->tile_shift = tile_shift;
+  p->rec_words = ((20 + 3 * k) + 3) & ~3u;
+  CK(cudaSetDevice(0));
+  CU(g_cu.moduleLoadData(&p->mod, cubin.data()));
+  CU(g_cu.moduleGetFunction(&p->setup, p->mod, "vgx_setup"));
+  CU(g_cu.moduleGetFunction(&p->raster, p->mod, "vgx_raster"));
+  *out = p;
+  return VGPU_OK;
+}
+
+extern "C" void vgpu_program_destroy(vgpu_program *p)
+{
+  if(!p)
+    return;
+  if(p->mod)
+    g_cu.moduleUnload(p->mod);
+  delete p;
+}
+
+extern "C" uint32_t vgpu_program_record_words(const vgpu_program *p) { return p->rec_words; }
+
+/* ------------------------------------------------------------------------ */
+/* command lists                                                             */
+/* ------------------------------------------------------------------------ */
+
+namespace
+{
+enum CmdType { CMD_COPY, CMD_CLEAR, CMD_DRAW };
+
+struct Cmd
+{
+  CmdType type;
+  void *dst = nullptr;
+  const void *src = nullptr;
+  u64 bytes = 0;
+  VgxTarget target;
+  int color = 0, depth = 0;
+  vgpu_program *prog = nullptr;
+  VgxDraw draw;
+};
+
+struct Job
+{
+  vgpu_program *prog = nullptr;
+  std::vector<VgxDraw> draws;
+  std::vector<VgxTarget> targets;
+  std::vector<u64> target_keys; /* colour address identifies a target */
+  u32 num_tris = 0, num_tiles = 0, key_bits = 1, all_tiles = 0;
+  /* device */
+  VgxDraw *d_draws = nullptr;
+  VgxTarget *d_targets = nullptr;
+  u64 rec_off = 0, cnt_off = 0; /* word offsets into the list's record/count arenas */
+  std::vector<u64> scan_levels; /* word offsets of scan scratch levels */
+};
+
+struct Exec
+{
+  enum { E_COPY, E_CLEAR, E_JOB, E_SEGMENT_END } kind;
+  size_t index; /* into cmds (copy/clear) or jobs */
+  VgxTarget target;
+  int color = 0, depth = 0;
+};
+}    // namespace
+
+struct vgpu_list
+{
+  std::vector<Cmd> cmds;
+  std::vector<std::pair<void *, std::pair<const void *, u64>>> uploads, downloads;
+  int mode = VGPU_MODE_BATCHED;
+  bool built = false;
+  std::vector<Job> jobs;
+  std::vector<Exec> plan;
+  u32 *d_records = nullptr;
+  u64 records_words = 0;
+  u32 *d_counts = nullptr;
+  u64 counts_words = 0;
+  u32 *h_totals = nullptr; /* pinned: pair totals per job */
+  u32 *d_totals = nullptr;
+  u64 tris_in = 0;
+};
+
+extern "C" vgpu_list *vgpu_list_create(void) { return new vgpu_list(); }
+
+static void list_free_device(vgpu_list *l)
+{
+  for(Job &j : l->jobs)
+  {
+    cudaFree(j.d_draws);
+    cudaFree(j.d_targets);
+  }
+  cudaFree(l->d_records);
+  cudaFree(l->d_counts);
+  cudaFree(l->d_totals);
+  cudaFreeHost(l->h_totals);
+  l->d_records = l->d_counts = l->d_totals = l->h_totals = nullptr;
+  l->jobs.clear();
+  l->plan.clear();
+  l->built = false;
+}
+
+extern "C" void vgpu_list_destroy(vgpu_list *l)
+{
+  if(!l)
+    return;
+  list_free_device(l);
+  delete l;
+}
+
+extern "C" void vgpu_list_copy(vgpu_list *l, void *dst, const void *src, uint64_t bytes)
+{
+  Cmd c;
+  c.type = CMD_COPY;
+  c.dst = dst;
+  c.src = src;
+  c.bytes = bytes;
+  l->cmds.push_back(c);
+  l->built = false;
+}
+
+extern "C" void vgpu_list_clear(vgpu_list *l, const VgxTarget *t, int color, int depth)
+{
+  Cmd c;
+  c.type = CMD_CLEAR;
+  c.target = *t;
+  c.color = color;
+  c.depth = depth;
+  l->cmds.push_back(c);
+  l->built = false;
+}
+
+extern "C" void vgpu_list_draw(vgpu_list *l, vgpu_program *prog, const VgxDraw *draw,
+                               const VgxTarget *target)
+{
+  Cmd c;
+  c.type = CMD_DRAW;
+  c.prog = prog;
+  c.draw = *draw;
+  c.target = *target;
+  l->cmds.push_back(c);
+  l->built = false;
+}
+
+extern "C" void vgpu_list_upload(vgpu_list *l, void *dev, const void *host, uint64_t bytes)
+{
+  l->uploads.push_back({dev, {host, bytes}});
+}
+
+extern "C" void vgpu_list_download(vgpu_list *l, void *host, const void *dev, uint64_t bytes)
+{
+  l->downloads.push_back({host, {dev, bytes}});
+}
+
+extern "C" void vgpu_list_set_mode(vgpu_list *l, int mode)
+{
+  if(l->mode != mode)
+  {
+    l->mode = mode;
+    list_free_device(l);
+  }
+}
+
+static u32 bits_for(u32 n)
+{
+  u32 b = 1;
+  while(b < 32 && (1ull << b) < n)
+    b++;
+  return b;
+}
+
+/* Form jobs and the execution plan, then upload the jobs' descriptors. */
+static int list_build(vgpu_list *l)
+{
+  list_free_device(l);
+  const bool batched = l->mode == VGPU_MODE_BATCHED;
+  std::map<u64, std::pair<VgxTarget, int>> pending_clear; /* colour address -> clear */
+  Job *open = nullptr;
+  auto close_job = [&]() { open = nullptr; };
+  auto flush_pending = [&]() {
+    for(auto &kv : pending_clear)
+    {
+      Exec e;
+      e.kind = Exec::E_CLEAR;
+      e.index = 0;
+      e.target = kv.second.first;
+      e.color = kv.second.second & 1;
+      e.depth = (kv.second.second >> 1) & 1;
+      l->plan.push_back(e);
+    }
+    pending_clear.clear();
+  };
+  l->tris_in = 0;
+  for(size_t ci = 0; ci < l->cmds.size(); ci++)
+  {
+    Cmd &c = l->cmds[ci];
+    if(c.type == CMD_COPY)
+    {
+      close_job();
+      flush_pending();
+      Exec e;
+      e.kind = Exec::E_SEGMENT_END;
+      e.index = 0;
+      l->plan.push_back(e);
+      e.kind = Exec::E_COPY;
+      e.index = ci;
+      l->plan.push_back(e);
+      e.kind = Exec::E_SEGMENT_END;
+      l->plan.push_back(e);
+      continue;
+    }
+    if(c.type == CMD_CLEAR)
+    {
+      if(!batched)
+      {
+        Exec e;
+        e.kind = Exec::E_CLEAR;
+        e.index = ci;
+        e.target = c.target;
+        e.color = c.color;
+        e.depth = c.depth;
+        l->plan.push_back(e);
+        continue;
+      }
+      /* a clear after draws to the same target in the open job ends that job */
+      if(open && std::find(open->target_keys.begin(), open->target_keys.end(), c.target.color) !=
+                     open->target_keys.end())
+        close_job();
+      auto it = pending_clear.find(c.target.color);
+      int flags = (c.color ? 1 : 0) | (c.depth ? 2 : 0);
+      if(it != pending_clear.end())
+        flags |= it->second.second;
+      pending_clear[c.target.color] = {c.target, flags};
+      continue;
+    }
+    /* draw */
+    u32 ntris = c.draw.num_tris;
+    l->tris_in += ntris;
+    if(!open || !batched || open->prog != c.prog)
+    {
+      l->jobs.emplace_back();
+      open = &l->jobs.back();
+      open->prog = c.prog;
+      Exec e;
+      e.kind = Exec::E_JOB;
+      e.index = l->jobs.size() - 1;
+      l->plan.push_back(e);
+    }
+    auto tk = std::find(open->target_keys.begin(), open->target_keys.end(), c.target.color);
+    u32 tidx;
+    if(tk == open->target_keys.end())
+    {
+      VgxTarget t = c.target;
+      t.init_clear = 0;
+      auto pc = pending_clear.find(t.color);
+      if(pc != pending_clear.end())
+      {
+        if(pc->second.second == 3 || (pc->second.second == 1 && !t.depth))
+        {
+          t.init_clear = 1;
+        }
+        else
+        {
+          /* partial clears stay separate kernels before the job */
+          Exec e;
+          e.kind = Exec::E_CLEAR;
+          e.target = pc->second.first;
+          e.color = pc->second.second & 1;
+          e.depth = (pc->second.second >> 1) & 1;
+          l->plan.insert(l->plan.end() - 1, e);
+        }
+        pending_clear.erase(pc);
+      }
+      t.tiles_x = (u32)(t.width + (1 << open->prog->tile_shift) - 1) >> open->prog->tile_shift;
+      t.tiles_y = (u32)(t.height + (1 << open->prog->tile_shift) - 1) >> open->prog->tile_shift;
+      t.tile_base = open->num_tiles;
+      open->num_tiles += t.tiles_x * t.tiles_y;
+      if(t.init_clear)
+        open->all_tiles = 1;
+      tidx = (u32)open->targets.size();
+      open->targets.push_back(t);
+      open->target_keys.push_back(t.color);
+    }
+    else
+    {
+      tidx = (u32)(tk - open->target_keys.begin());
+    }
+    VgxDraw d = c.draw;
+    d.target = tidx;
+    d.tri_base = open->num_tris;
+    open->num_tris += ntris;
+    open->draws.push_back(d);
+  }
+  close_job();
+  flush_pending();
+
+  /* drop empty jobs' work but keep their fused clears: a job with no triangles still rasters */
+  u64 rec_words = 0, cnt_words = 0;
+  for(Job &j : l->jobs)
+  {
+    j.key_bits = bits_for(std::max(j.num_tiles, 2u));
+    j.rec_off = rec_words;
+    rec_words += (u64)j.num_tris * j.prog->rec_words;
+    j.cnt_off = cnt_words;
+    cnt_words += (u64)j.num_tris + 1;
+    /* scan scratch levels after the counts */
+    u64 n = (u64)j.num_tris + 1;
+    while(n > (u64)kScanTile)
+    {
+      n = (n + kScanTile - 1) / kScanTile;
+      j.scan_levels.push_back(cnt_words);
+      cnt_words += n + 1;
+    }
+    CK(cudaMalloc(&j.d_draws, std::max<size_t>(1, j.draws.size()) * sizeof(VgxDraw)));
+    CK(cudaMalloc(&j.d_targets, std::max<size_t>(1, j.targets.size()) * sizeof(VgxTarget)));
+    CK(cudaMemcpy(j.d_draws, j.draws.data(), j.draws.size() * sizeof(VgxDraw), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(j.d_targets, j.targets.data(), j.targets.size() * sizeof(VgxTarget),
+                  cudaMemcpyHostToDevice));
+  }
+  l->records_words = rec_words;
+  l->counts_words = cnt_words;
+  CK(cudaMalloc(&l->d_records, std::max<u64>(4, rec_words) * 4));
+  CK(cudaMalloc(&l->d_counts, std::max<u64>(4, cnt_words) * 4));
+  CK(cudaMalloc(&l->d_totals, std::max<size_t>(1, l->jobs.size()) * 4));
+  CK(cudaMallocHost(&l->h_totals, std::max<size_t>(1, l->jobs.size()) * 4));
+  l->built = true;
+  return VGPU_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* queues                                                                    */
+/* ------------------------------------------------------------------------ */
+
+struct vgpu_queue
+{
+  cudaStream_t stream = nullptr;
+  u32 *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr};
+  u32 pair_capacity = 0;
+  u32 *tstart = nullptr, *tend = nullptr, *work = nullptr;
+  u32 tile_capacity = 0;
+  u32 *hist = nullptr;
+  u64 hist_words = 0;
+  u32 *scratch = nullptr;
+  u64 scratch_words = 0;
+  u32 *status = nullptr;  /* 4 words per job slot */
+  u64 *counters = nullptr; /* tris_out, tested, covered, shaded */
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  vgpu_stats stats;
+  u64 launches = 0;
+  bool timed = false;
+};
+
+struct vgpu_fence
+{
+  cudaEvent_t ev = nullptr;
+  bool pending = false;
+  vgpu_queue *q = nullptr;
+};
+
+extern "C" int vgpu_queue_create(vgpu_queue **out)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return rc;
+  vgpu_queue *q = new vgpu_queue();
+  CK(cudaStreamCreateWithFlags(&q->stream, cudaStreamNonBlocking));
+  CK(cudaMalloc(&q->status, 64));
+  CK(cudaMemset(q->status, 0, 64));
+  CK(cudaMalloc(&q->counters, 4 * sizeof(u64)));
+  CK(cudaMemset(q->counters, 0, 4 * sizeof(u64)));
+  CK(cudaEventCreate(&q->ev0));
+  CK(cudaEventCreate(&q->ev1));
+  memset(&q->stats, 0, sizeof(q->stats));
+  *out = q;
+  return VGPU_OK;
+}
+
+extern "C" void vgpu_queue_destroy(vgpu_queue *q)
+{
+  if(!q)
+    return;
+  cudaStreamSynchronize(q->stream);
+  for(int i = 0; i < 2; i++)
+  {
+    cudaFree(q->keys[i]);
+    cudaFree(q->vals[i]);
+  }
+  cudaFree(q->tstart);
+  cudaFree(q->tend);
+  cudaFree(q->work);
+  cudaFree(q->hist);
+  cudaFree(q->scratch);
+  cudaFree(q->status);
+  cudaFree(q->counters);
+  cudaEventDestroy(q->ev0);
+  cudaEventDestroy(q->ev1);
+  cudaStreamDestroy(q->stream);
+  delete q;
+}
+
+extern "C" void *vgpu_queue_stream(vgpu_queue *q) { return (void *)q->stream; }
+
+static int ensure_pairs(vgpu_queue *q, u32 need)
+{
+  if(need <= q->pair_capacity)
+    return VGPU_OK;
+  u32 cap = std::max<u32>(need + need / 4, 1u << 20);
+  for(int i = 0; i < 2; i++)
+  {
+    cudaFree(q->keys[i]);
+    cudaFree(q->vals[i]);
+    CK(cudaMalloc(&q->keys[i], (size_t)cap * 4));
+    CK(cudaMalloc(&q->vals[i], (size_t)cap * 4));
+  }
+  q->pair_capacity = cap;
+  u64 nb = ((u64)cap + kSortTile - 1) / kSortTile;
+  u64 hw = nb * 256 + 1;
+  if(hw > q->hist_words)
+  {
+    cudaFree(q->hist);
+    CK(cudaMalloc(&q->hist, hw * 4));
+    q->hist_words = hw;
+  }
+  return VGPU_OK;
+}
+
+static int ensure_tiles(vgpu_queue *q, u32 tiles)
+{
+  if(tiles <= q->tile_capacity)
+    return VGPU_OK;
+  u32 cap = std::max<u32>(tiles, 1u << 16);
+  cudaFree(q->tstart);
+  cudaFree(q->tend);
+  cudaFree(q->work);
+  CK(cudaMalloc(&q->tstart, (size_t)cap * 4));
+  CK(cudaMalloc(&q->tend, (size_t)cap * 4));
+  CK(cudaMalloc(&q->work, (size_t)cap * 4));
+  q->tile_capacity = cap;
+  return VGPU_OK;
+}
+
+static int ensure_scratch(vgpu_queue *q, u64 words)
+{
+  if(words <= q->scratch_words)
+    return VGPU_OK;
+  cudaFree(q->scratch);
+  CK(cudaMalloc(&q->scratch, words * 4));
+  q->scratch_words = words;
+  return VGPU_OK;
+}
+
+/* exclusive scan of in[0..n) into out[0..n], out[n] = total; levels = word offsets in `base` */
+static int scan_u32(vgpu_queue *q, const u32 *in, u32 *out, u64 n, u32 *base,
+                    const std::vector<u64> &levels, size_t level)
+{
+  u64 nb = (n + kScanTile - 1) / kScanTile;
+  if(nb <= 1)
+  {
+    k_scan_apply<<<1, kScanBlock, 0, q->stream>>>(in, out, (u32)n, nullptr, 1);
+    q->launches++;
+    return VGPU_OK;
+  }
+  u32 *sums = base + levels[level];
+  k_scan_reduce<<<(unsigned)nb, kScanBlock, 0, q->stream>>>(in, (u32)n, sums);
+  int rc = scan_u32(q, sums, sums, nb, base, levels, level + 1);
+  if(rc)
+    return rc;
+  k_scan_apply<<<(unsigned)nb, kScanBlock, 0, q->stream>>>(in, out, (u32)n, sums, 1);
+  q->launches += 2;
+  return VGPU_OK;
+}
+
+static VgxJob make_job(vgpu_queue *q, vgpu_list *l, Job &j, size_t ji)
+{
+  VgxJob J;
+  memset(&J, 0, sizeof(J));
+  J.draws = (u64)j.d_draws;
+  J.targets = (u64)j.d_targets;
+  J.records = (u64)(l->d_records + j.rec_off);
+  J.counts = (u64)(l->d_counts + j.cnt_off);
+  J.keys = (u64)q->keys[0];
+  J.vals = (u64)q->vals[0];
+  J.keys_alt = (u64)q->keys[1];
+  J.vals_alt = (u64)q->vals[1];
+  J.tile_start = (u64)q->tstart;
+  J.tile_end = (u64)q->tend;
+  J.work = j.all_tiles ? 0 : (u64)q->work;
+  J.status = (u64)q->status;
+  J.counters = (u64)q->counters;
+  J.scratch = (u64)q->scratch;
+  J.num_draws = (u32)j.draws.size();
+  J.num_tris = j.num_tris;
+  J.num_targets = (u32)j.targets.size();
+  J.num_tiles = j.num_tiles;
+  J.pair_capacity = q->pair_capacity;
+  J.tile_shift = j.prog->tile_shift;
+  J.key_bits = j.key_bits;
+  J.all_tiles = j.all_tiles;
+  (void)ji;
+  return J;
+}
+
+static int launch(vgpu_queue *q, CUfunction f, unsigned grid, unsigned block, VgxJob *J)
+{
+  void *args[] = {J};
+  CU(g_cu.launchKernel(f, grid, 1, 1, block, 1, 1, 0, (CUstream)q->stream, args, nullptr));
+  q->launches++;
+  return VGPU_OK;
+}
+
+/* phase A of a job: setup + scan of tile counts; total pairs -> d_totals[ji] */
+static int run_setup(vgpu_queue *q, vgpu_list *l, size_t ji)
+{
+  Job &j = l->jobs[ji];
+  if(j.num_tris == 0)
+  {
+    CK(cudaMemsetAsync(l->d_totals + ji, 0, 4, q->stream));
+    return VGPU_OK;
+  }
+  VgxJob J = make_job(q, l, j, ji);
+  int rc = launch(q, j.prog->setup, (j.num_tris + 255) / 256, 256, &J);
+  if(rc)
+    return rc;
+  u32 *counts = l->d_counts + j.cnt_off;
+  rc = scan_u32(q, counts, counts, j.num_tris, l->d_counts, j.scan_levels, 0);
+  if(rc)
+    return rc;
+  CK(cudaMemcpyAsync(l->d_totals + ji, counts + j.num_tris, 4, cudaMemcpyDeviceToDevice, q->stream));
+  return VGPU_OK;
+}
+
+/* phase B of a job: bin, sort, ranges, raster */
+static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
+{
+  Job &j = l->jobs[ji];
+  int rc = ensure_tiles(q, j.num_tiles);
+  if(rc)
+    return rc;
+  VgxJob J = make_job(q, l, j, ji);
+  u32 *counts = l->d_counts + j.cnt_off;
+  const u32 total = l->h_totals[ji];
+  CK(cudaMemsetAsync(q->status + 1, 0, 12, q->stream)); /* pair total, queue, work count */
+  if(j.all_tiles || total)
+  {
+    CK(cudaMemsetAsync(q->tstart, 0, (size_t)j.num_tiles * 4, q->stream));
+    CK(cudaMemsetAsync(q->tend, 0, (size_t)j.num_tiles * 4, q->stream));
+  }
+  if(total)
+  {
+    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.prog->rec_words, counts);
+    q->launches++;
+    /* radix sort by tile id */
+    u32 nb = (total + kSortTile - 1) / kSortTile;
+    int src = 0;
+    for(u32 shift = 0; shift < j.key_bits; shift += 8)
+    {
+      k_radix_hist<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], total, shift, q->hist, nb);
+      std::vector<u64> lv;
+      u64 n = (u64)nb * 256;
+      u64 need = 0;
+      {
+        u64 m = n;
+        while(m > (u64)kScanTile)
+        {
+          m = (m + kScanTile - 1) / kScanTile;
+          lv.push_back(need);
+          need += m + 1;
+        }
+      }
+      rc = ensure_scratch(q, need + 4);
+      if(rc)
+        return rc;
+      rc = scan_u32(q, q->hist, q->hist, n, q->scratch, lv, 0);
+      if(rc)
+        return rc;
+      k_radix_scatter<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], q->vals[src], total, shift,
+                                                        q->hist, nb, q->keys[src ^ 1],
+                                                        q->vals[src ^ 1]);
+      q->launches += 2;
+      src ^= 1;
+    }
+    J.keys = (u64)q->keys[src];
+    J.vals = (u64)q->vals[src];
+    CK(cudaMemcpyAsync(q->status + 1, counts + j.num_tris, 4, cudaMemcpyDeviceToDevice, q->stream));
+    unsigned rg = std::min<u32>((total + 255) / 256, (u32)g_sms * 8);
+    k_ranges<<<rg, 256, 0, q->stream>>>(q->keys[src], q->status + 1, q->pair_capacity, q->tstart,
+                                        q->tend, j.all_tiles ? nullptr : q->work, q->status);
+    q->launches++;
+  }
+  if(!j.all_tiles && !total)
+    return VGPU_OK;
+  unsigned grid = std::max(1u, (unsigned)g_sms * g_tuning.raster_blocks_per_sm);
+  u32 warps_needed = j.all_tiles ? j.num_tiles : total;
+  const unsigned warps = j.prog->rec_words > 40 ? 4 : 8; /* VGX_RASTER_WARPS */
+  grid = std::min<unsigned>(grid, (warps_needed + warps - 1) / warps);
+  grid = std::max(grid, 1u);
+  return launch(q, j.prog->raster, grid, warps * 32, &J);
+}
+
+extern "C" int vgpu_submit(vgpu_queue *q, vgpu_list *l)
+{
+  if(!l->built)
+  {
+    int rc = list_build(l);
+    if(rc)
+      return rc;
+  }
+  CK(cudaEventRecord(q->ev0, q->stream));
+  for(auto &u : l->uploads)
+    CK(cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, q->stream));
+  size_t p = 0;
+  while(p < l->plan.size())
+  {
+    /* a segment runs to the next copy */
+    size_t e = p;
+    while(e < l->plan.size() && l->plan[e].kind != Exec::E_SEGMENT_END &&
+          l->plan[e].kind != Exec::E_COPY)
+      e++;
+    /* phase A: setups */
+    bool any_job = false;
+    for(size_t i = p; i < e; i++)
+      if(l->plan[i].kind == Exec::E_JOB)
+      {
+        int rc = run_setup(q, l, l->plan[i].index);
+        if(rc)
+          return rc;
+        any_job = true;
+      }
+    if(any_job)
+    {
+      /* one synchronisation per segment: pair totals size the sort storage */
+      CK(cudaMemcpyAsync(l->h_totals, l->d_totals, l->jobs.size() * 4, cudaMemcpyDeviceToHost,
+                         q->stream));
+      CK(cudaStreamSynchronize(q->stream));
+      u32 mx = 0;
+      for(size_t i = p; i < e; i++)
+        if(l->plan[i].kind == Exec::E_JOB)
+          mx = std::max(mx, l->h_totals[l->plan[i].index]);
+      int rc = ensure_pairs(q, mx);
+      if(rc)
+        return rc;
+    }
+    /* phase B: clears, binning and raster in command order */
+    for(size_t i = p; i < e; i++)
+    {
+      const Exec &x = l->plan[i];
+      if(x.kind == Exec::E_CLEAR)
+      {
+        u64 n = (u64)x.target.width * x.target.height;
+        unsigned g = (unsigned)std::min<u64>((n + 255) / 256, (u64)g_sms * 16);
+        k_clear<<<std::max(g, 1u), 256, 0, q->stream>>>(x.target, x.color, x.depth);
+        q->launches++;
+      }
+      else if(x.kind == Exec::E_JOB)
+      {
+        int rc = run_raster(q, l, x.index);
+        if(rc)
+          return rc;
+      }
+    }
+    if(e < l->plan.size() && l->plan[e].kind == Exec::E_COPY)
+    {
+      const Cmd &c = l->cmds[l->plan[e].index];
+      CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, q->stream));
+    }
+    p = e + 1;
+  }
+  for(auto &d : l->downloads)
+    CK(cudaMemcpyAsync(d.first, d.second.first, d.second.second, cudaMemcpyDeviceToHost, q->stream));
+  CK(cudaEventRecord(q->ev1, q->stream));
+  q->timed = true;
+  q->stats.tris_in += l->tris_in;
+  q->stats.draws += 0;
+  for(const Cmd &c : l->cmds)
+    if(c.type == CMD_DRAW)
+      q->stats.draws++;
+  q->stats.jobs += l->jobs.size();
+  CK(cudaGetLastError());
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_fence_create(vgpu_fence **out)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return rc;
+  vgpu_fence *f = new vgpu_fence();
+  CK(cudaEventCreateWithFlags(&f->ev, cudaEventDisableTiming));
+  *out = f;
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_fence_signal(vgpu_queue *q, vgpu_fence *f)
+{
+  CK(cudaEventRecord(f->ev, q->stream));
+  f->pending = true;
+  f->q = q;
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_fence_status(vgpu_fence *f)
+{
+  if(!f->pending)
+    return VGPU_OK;
+  cudaError_t e = cudaEventQuery(f->ev);
+  if(e == cudaErrorNotReady)
+    return VGPU_TIMEOUT;
+  if(e != cudaSuccess)
+    return VGPU_ERROR_DEVICE_LOST;
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_fence_wait(vgpu_fence *f, uint64_t timeout_ns)
+{
+  if(!f->pending)
+    return VGPU_OK;
+  if(timeout_ns == ~0ull)
+  {
+    CK(cudaEventSynchronize(f->ev));
+    return VGPU_OK;
+  }
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  for(;;)
+  {
+    int s = vgpu_fence_status(f);
+    if(s != VGPU_TIMEOUT)
+      return s;
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    u64 el = (u64)(t1.tv_sec - t0.tv_sec) * 1000000000ull + (u64)(t1.tv_nsec - t0.tv_nsec);
+    if(el >= timeout_ns)
+      return VGPU_TIMEOUT;
+  }
+}
+
+extern "C" void vgpu_fence_reset(vgpu_fence *f) { f->pending = false; }
+
+extern "C" void vgpu_fence_destroy(vgpu_fence *f)
+{
+  if(!f)
+    return;
+  cudaEventDestroy(f->ev);
+  delete f;
+}
+
+extern "C" int vgpu_queue_wait_idle(vgpu_queue *q)
+{
+  CK(cudaStreamSynchronize(q->stream));
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out)
+{
+  CK(cudaStreamSynchronize(q->stream));
+  u64 c[4];
+  CK(cudaMemcpy(c, q->counters, sizeof(c), cudaMemcpyDeviceToHost));
+  u32 st = 0;
+  CK(cudaMemcpy(&st, q->status, 4, cudaMemcpyDeviceToHost));
+  *out = q->stats;
+  out->tris_out = c[0];
+  out->tested = c[1];
+  out->covered = c[2];
+  out->shaded = c[3];
+  out->status = st;
+  out->kernel_launches = q->launches;
+  float ms = 0.0f;
+  if(q->timed && cudaEventElapsedTime(&ms, q->ev0, q->ev1) == cudaSuccess)
+    out->gpu_ms = ms;
+  return VGPU_OK;
+}
+
+extern "C" void vgpu_queue_reset_stats(vgpu_queue *q)
+{
+  cudaStreamSynchronize(q->stream);
+  cudaMemset(q->counters, 0, 4 * sizeof(u64));
+  cudaMemset(q->status, 0, 4);
+  memset(&q->stats, 0, sizeof(q->stats));
+  q->launches = 0;
+}
+
+extern "C" void vgpu_set_tuning(const vgpu_tuning *t) { g_tuning = *t; }
+extern "C" void vgpu_get_tuning(vgpu_tuning *t) { *t = g_tuning; }

@@ -781,3 +781,5 @@ extern "C" void vsd_release(vsd_scene *s)
   if(s->fence) f.vkDestroyFence(d, s->fence, nullptr);
   delete s;
 }
+
+extern "C" void *vsd_queue(vsd_context *c) { return (void *)c->queue; }
