@@ -198,7 +198,8 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
 #endif
           r[R_LOD] = __float_as_int(lod);
           const bool depth_test = D.depth_op != 7u && T.depth != 0;
-          u32 st = (D.depth_op & 7u) | (depth_test && D.depth_write ? S_DEPTH_WRITE : 0u) |
+          /* depth writes do not depend on the compare op (rasterizer.cpp:680-683) */
+          u32 st = (D.depth_op & 7u) | (T.depth != 0 && D.depth_write ? S_DEPTH_WRITE : 0u) |
                    (D.blend_enable ? S_BLEND : 0u) | ((D.src_factor & 31u) << 5) |
                    ((D.dst_factor & 31u) << 10) | (depth_test ? S_DEPTH_TEST : 0u) |
                    ((D.blend_op & 7u) << 16);
