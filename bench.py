@@ -1,0 +1,344 @@
+"""Benchmark of the Visor draw path on GB300.
+
+Workload (the configuration the headline metric is quoted on): 1920x1080
+RGBA8 + D32, one non-indexed draw of 1,000,000 seeded screen-space triangles
+(area log-uniform 1-10,000 px, random orientation, per-vertex depth U[0,1],
+RGBA8 colour with alpha U[0.2,1]), pass-through shaders, depth LESS_OR_EQUAL
+with writes, SRC_ALPHA / ONE_MINUS_SRC_ALPHA blending in primitive order.
+
+A step is one vkQueueSubmit of the recorded command buffer and its fence wait.
+  value   shaded Gfrag/s with inputs resident in HBM (device-local vertex
+          buffer and render targets); device time from CUDA events recorded on
+          the submitting stream; L2 flushed (512 MiB write) between steps.
+  e2e     the same metric through the Vulkan API with host buffers: every
+          submit copies the vertex buffer from host-visible (pinned) staging
+          and the render targets are host-visible, so the colour and depth
+          images come back to the host inside the timed region.
+Shaded fragment = fragment that passed the early depth test
+(rasterizer/depth/passed, rasterizer.cpp:678); triangles = triangles in.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+SEED = 20260101
+WORKLOAD = ("1920x1080 RGBA8+D32, 1,000,000 screen-space triangles (area log-uniform 1-1e4 px), "
+            "blend SRC_ALPHA/ONE_MINUS_SRC_ALPHA, depth LEQUAL + write, one vkCmdDraw")
+METRIC = "shaded Gfrags/s"
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def _traffic_from_profile():
+    """dram bytes (read + write) per raster launch recorded from ncu (profiles/), scaled to
+    the full workload when the capture used a smaller one."""
+    path = os.path.join(HERE, "profiles", "raster_cfg2_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_full_launch:"):
+                return int(float(line.split(":", 1)[1]))
+    except Exception:
+        pass
+    return None
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+        return dist, rank, world
+    return None, rank, world
+
+
+def _max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(threads=None, sample_tris=None):
+    """The oracle port of the reference's CPU draw path on this host's cores, one full frame."""
+    from oracle import loader
+    o = loader.Oracle()
+    params = {}
+    if sample_tris:
+        params["count"] = sample_tris
+    h = o.generate(2, SEED, **params)
+    threads = threads or (os.cpu_count() or 1)
+    t0 = time.time()
+    _, _, k = o.render(h, threads=threads)
+    dt = time.time() - t0
+    return {"value": k["shaded"] / dt / 1e9, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"one full frame of the workload ({k['tris_in']} triangles, {k['shaded']} shaded "
+                      f"fragments) rendered by the C restatement in {threads} row bands, {dt:.2f} s",
+            "seconds": dt, "mtris_per_s": k["tris_in"] / dt / 1e6}
+
+
+def run_reference(args):
+    dist, rank, world = _dist()
+    if rank != 0:
+        return 0
+    from oracle import loader
+    threads = os.cpu_count() or 1
+    kind = "port"
+    o = loader.Oracle()
+    h = o.generate(2, SEED)
+    for _ in range(args.warmup):
+        o.render(h, threads=threads)
+    times, shaded, tris = [], 0, 0
+    for _ in range(args.steps):
+        t0 = time.time()
+        _, _, k = o.render(h, threads=threads)
+        times.append(time.time() - t0)
+        shaded, tris = k["shaded"], k["tris_in"]
+    ms = 1e3 * sum(times) / len(times)
+    value = shaded / (ms / 1e3) / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "seed": SEED, "threads": threads},
+        "mtris_per_s": tris / (ms / 1e3) / 1e6,
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
+                         "sample": f"full frame per step; the reference's draw path restated in C "
+                                   f"(oracle/visor_oracle.c) split into {threads} row bands"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import visor_gb300 as vg
+    from visor_gb300 import scene as vs
+
+    dist, rank, world = _dist()
+    vg.set_tuning(time_raster=1)
+    dev = vg.Device()
+    params = {"count": args.triangles} if args.triangles else {}
+    h = vs.generate(vg.lib(), vs.CFG_TRIS, SEED, **params)
+    w, hgt = h.targets()[0]
+    tris = h.triangle_count()
+
+    results = {}
+    modes = [("batched", vg.MODE_BATCHED)]
+    if not args.only_batched:
+        modes.append(("per_draw", vg.MODE_PER_DRAW))
+    for mode_name, mode in modes:
+        vg.set_mode(mode)
+        up = dev.upload(h, vg.DEVICE_TARGETS)
+        for _ in range(args.warmup):
+            up.submit()
+        gpu_ms, raster_ms, shaded, covered, launches = [], [], 0, 0, 0
+        clocks = Clocks(_env_int("LOCAL_RANK", 0))
+        if dist:
+            dist.barrier()
+        with clocks if mode_name == "batched" else _Null():
+            for _ in range(args.steps):
+                dev.flush_l2()
+                dev.reset_stats()
+                up.submit()
+                st = dev.stats()
+                gpu_ms.append(st["gpu_ms"])
+                raster_ms.append(st["raster_ms"])
+                shaded, covered = st["shaded"], st["covered"]
+                launches += st["kernel_launches"]
+        if dist:
+            dist.barrier()
+        up.release()
+        ms = sum(gpu_ms) / len(gpu_ms)
+        results[mode_name] = {"ms": ms, "raster_ms": sum(raster_ms) / len(raster_ms),
+                              "shaded": shaded, "covered": covered, "launches": launches,
+                              "clocks": clocks.summary() if mode_name == "batched" else None}
+
+    # end to end through the Vulkan API with host buffers
+    walls, h2d = [1.0], 0
+    if not args.only_batched:
+        vg.set_mode(vg.MODE_BATCHED)
+        up = dev.upload(h, vg.RESTAGE_INPUTS)
+        for _ in range(args.warmup):
+            up.submit()
+        walls = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            up.submit()
+            walls.append(time.perf_counter() - t0)
+        h2d = up.restage_bytes()
+        up.release()
+    else:
+        results["per_draw"] = results["batched"]
+    dev.close()
+
+    b = results["batched"]
+    ms = _max_over_ranks(dist, b["ms"])
+    e2e_s = _max_over_ranks(dist, sum(walls) / len(walls))
+    shaded_all = _sum_over_ranks(dist, b["shaded"])
+    value = shaded_all / (ms / 1e3) / 1e9
+    per_draw_ms = _max_over_ranks(dist, results["per_draw"]["ms"])
+
+    # roofline of the dominant kernel (raster): algorithmic bytes per launch
+    # = clear (fused) + 4 B depth read per covered fragment + (4 B colour write
+    #   + 4 B depth write + 4 B colour read for blending) per shaded fragment
+    alg_bytes = w * hgt * 8 + b["covered"] * 4 + b["shaded"] * 12
+    peaks = _peaks()
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = alg_bytes / (b["raster_ms"] / 1e3) / 1e9 if b["raster_ms"] > 0 else None
+    frame_bytes = tris * 3 * 20 + alg_bytes  # full-frame model incl. vertex fetch
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "seed": SEED, "width": w, "height": hgt, "triangles": tris,
+                   "mode": "batched", "l2": "flushed between steps (512 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "mtris_per_s": world * tris / (ms / 1e3) / 1e6,
+        "covered_gfrags_per_s": world * b["covered"] / (ms / 1e3) / 1e9,
+        "per_draw": {"value": world * results["per_draw"]["shaded"] / (per_draw_ms / 1e3) / 1e9,
+                     "ms_per_step": per_draw_ms, "note": "same workload, per-draw launch path"},
+        "e2e": {"value": shaded_all / e2e_s / 1e9, "unit": METRIC, "ms_per_step": e2e_s * 1e3,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": w * hgt * 8,
+                "path": "vkQueueSubmit + vkWaitForFences, host-visible staging and targets"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": _traffic_from_profile(),
+                     "kernel": "vgx_raster", "kernel_ms": b["raster_ms"],
+                     "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
+                     "frame_model_gbs": frame_bytes / (ms / 1e3) / 1e9},
+        "clocks": b["clocks"],
+        "gpu_launches": b["launches"],
+        "shaded_per_step": b["shaded"], "covered_per_step": b["covered"],
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline()
+        except Exception as e:  # reported, never fatal to the GPU number
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--triangles", type=int, default=0,
+                    help="smaller triangle count of the same workload (profiling captures)")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="time only the batched device-resident path (profiling captures)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -112,11 +112,14 @@ int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out);
 void vgpu_queue_reset_stats(vgpu_queue *q);
 /* Stream the queue launches on (cudaStream_t), for callers that time around it. */
 void *vgpu_queue_stream(vgpu_queue *q);
+/* Overwrite a buffer larger than L2 on the queue's stream (benchmark hygiene). */
+int vgpu_queue_flush_l2(vgpu_queue *q);
 
 /* Tuning knobs read at list build time (autotuner, see tune.py). */
 typedef struct vgpu_tuning {
   uint32_t raster_blocks_per_sm; /* persistent raster CTAs per SM */
   uint32_t use_graphs;           /* replay batched lists as CUDA graphs */
+  uint32_t time_raster;          /* record CUDA events around raster launches (vgpu_stats.raster_ms) */
 } vgpu_tuning;
 void vgpu_set_tuning(const vgpu_tuning *t);
 void vgpu_get_tuning(vgpu_tuning *t);

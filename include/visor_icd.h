@@ -45,6 +45,8 @@ int visor_gb300_get_mode(void);
 /* Queue statistics (rasterizer counters, launches, device time of the last submit). */
 int visor_gb300_queue_stats(VkQueue queue, vgpu_stats *out);
 void visor_gb300_queue_reset_stats(VkQueue queue);
+/* Overwrite a buffer larger than L2 on the queue (benchmark hygiene between timed steps). */
+int visor_gb300_flush_l2(VkQueue queue);
 
 /* SPIR-V pair -> CUDA source, without a device (returns 0 and err on failure). */
 size_t visor_gb300_translate(const uint32_t *vs_words, size_t vs_count, const uint32_t *fs_words,

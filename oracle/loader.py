@@ -52,6 +52,9 @@ class Oracle:
         self.lib.vor_render_passes.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                                C.POINTER(Counters)]
         self.lib.vor_render_passes.restype = C.c_int
+        self.lib.vor_render_threads.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                                C.POINTER(Counters), C.c_uint32]
+        self.lib.vor_render_threads.restype = C.c_int
         self.lib.vor_sample_bilinear.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_float,
                                                  C.c_float, C.POINTER(C.c_float)]
         self.lib.vor_log2.argtypes = [C.c_float]
@@ -60,11 +63,14 @@ class Oracle:
     def generate(self, config, seed, **params):
         return vscene.generate(self.lib, config, seed, **params)
 
-    def render(self, handle, passes=None):
+    def render(self, handle, passes=None, threads=0):
         cols, deps = vscene.target_buffers(handle)
         cp, dp = vscene.pointer_arrays(cols, deps)
         cnt = Counters()
-        if passes is None:
+        if threads:
+            first, count = passes if passes else (0, handle.s.num_passes)
+            rc = self.lib.vor_render_threads(handle.ptr, first, count, cp, dp, C.byref(cnt), threads)
+        elif passes is None:
             rc = self.lib.vor_render(handle.ptr, cp, dp, C.byref(cnt))
         else:
             rc = self.lib.vor_render_passes(handle.ptr, passes[0], passes[1], cp, dp, C.byref(cnt))

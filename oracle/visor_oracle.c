@@ -17,6 +17,7 @@
 
 #include <limits.h>
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -44,6 +45,8 @@ typedef struct draw_ctx {
   uint8_t *col;
   float *depth;
   vor_counters *cnt;
+  int band_y0, band_y1; /* rows [band_y0, band_y1) this context renders */
+  int count_prims;      /* 1: this context counts triangles and draws */
 } draw_ctx;
 
 typedef struct tri_ctx {
@@ -638,7 +641,8 @@ static void draw_triangles(draw_ctx *c)
     for(int k = 0; k < 3; k++)
       to_window(c->w, c->h, &v[k].position, &wx[k], &wy[k]);
 
-    c->cnt->tris_in++;
+    if(c->count_prims)
+      c->cnt->tris_in++;
 
     /* double_triarea, rasterizer.cpp:272-275 */
     int area2 = (wx[1] - wx[0]) * (wy[2] - wy[0]) - (wy[1] - wy[0]) * (wx[2] - wx[0]);
@@ -662,7 +666,8 @@ static void draw_triangles(draw_ctx *c)
       area2_flipped *= -1;
     }
 
-    c->cnt->tris_out++;
+    if(c->count_prims)
+      c->cnt->tris_out++;
 
     /* MinMax + clamp, rasterizer.cpp:428-435 */
     int minx = INT_MAX, miny = INT_MAX, maxx = INT_MIN, maxy = INT_MIN;
@@ -677,6 +682,11 @@ static void draw_triangles(draw_ctx *c)
     miny = miny > 0 ? miny : 0;
     maxx = maxx < w - 1 ? maxx : w - 1;
     maxy = maxy < h - 1 ? maxy : h - 1;
+    /* a band renderer only touches its rows; the union over bands is the frame */
+    if(miny < c->band_y0)
+      miny = c->band_y0;
+    if(maxy > c->band_y1)
+      maxy = c->band_y1;
 
     /* TriangleWork setup, rasterizer.cpp:437-452 */
     float invarea = 1.0f / (float)area2_flipped;
@@ -700,12 +710,22 @@ static void draw_triangles(draw_ctx *c)
     process_triangle(c, &tc, wx, wy, area2, barymul, invarea, invw, depth, minx, miny, maxx,
                      maxy);
   }
-  c->cnt->draws++;
+  if(c->count_prims)
+    c->cnt->draws++;
   free(vs);
 }
 
+static int render_band(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
+                       float **depths, vor_counters *counters, int y0, int y1, int count_prims);
+
 int vor_render_passes(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
                       float **depths, vor_counters *counters)
+{
+  return render_band(s, first, count, colors, depths, counters, 0, INT_MAX, 1);
+}
+
+static int render_band(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
+                       float **depths, vor_counters *counters, int y0, int y1, int count_prims)
 {
   vor_counters local;
   memset(&local, 0, sizeof(local));
@@ -718,8 +738,13 @@ int vor_render_passes(const vsc_scene *s, uint32_t first, uint32_t count, uint8_
     /* BeginRenderPass, cmd_exec.cpp:35-64 */
     if(pass->clear)
     {
-      clear_color(col, tg->width, tg->height, s->clear_color);
-      clear_depth(dep, tg->width, tg->height, s->clear_depth);
+      int r0 = y0 < (int)tg->height ? y0 : (int)tg->height;
+      int r1 = y1 < (int)tg->height ? y1 : (int)tg->height;
+      if(r1 > r0)
+      {
+        clear_color(col + (uint64_t)r0 * tg->width * 4, tg->width, (uint32_t)(r1 - r0), s->clear_color);
+        clear_depth(dep + (uint64_t)r0 * tg->width, tg->width, (uint32_t)(r1 - r0), s->clear_depth);
+      }
     }
     for(uint32_t di = pass->first_draw; di < pass->first_draw + pass->draw_count; di++)
     {
@@ -738,6 +763,9 @@ int vor_render_passes(const vsc_scene *s, uint32_t first, uint32_t count, uint8_
       c.col = col;
       c.depth = dep;
       c.cnt = &local;
+      c.band_y0 = y0;
+      c.band_y1 = y1;
+      c.count_prims = count_prims;
       draw_triangles(&c);
     }
   }
@@ -749,4 +777,69 @@ int vor_render_passes(const vsc_scene *s, uint32_t first, uint32_t count, uint8_
 int vor_render(const vsc_scene *s, uint8_t **colors, float **depths, vor_counters *counters)
 {
   return vor_render_passes(s, 0, s->num_passes, colors, depths, counters);
+}
+
+typedef struct band_job {
+  const vsc_scene *s;
+  uint32_t first, count;
+  uint8_t **colors;
+  float **depths;
+  vor_counters cnt;
+  int y0, y1, count_prims;
+} band_job;
+
+static void *band_main(void *arg)
+{
+  band_job *j = (band_job *)arg;
+  render_band(j->s, j->first, j->count, j->colors, j->depths, &j->cnt, j->y0, j->y1, j->count_prims);
+  return NULL;
+}
+
+/*
+ * Multi-threaded CPU baseline: `threads` workers each render every triangle of
+ * the selected passes restricted to one horizontal band of rows.  Every pixel
+ * still sees its triangles in primitive order, so the output is identical to
+ * the serial oracle; the vertex work is repeated per band.
+ */
+int vor_render_threads(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
+                       float **depths, vor_counters *counters, uint32_t threads)
+{
+  uint32_t maxh = 1;
+  for(uint32_t t = 0; t < s->num_targets; t++)
+    maxh = s->targets[t].height > maxh ? s->targets[t].height : maxh;
+  if(threads < 1)
+    threads = 1;
+  if(threads > maxh)
+    threads = maxh;
+  band_job *jobs = (band_job *)calloc(threads, sizeof(band_job));
+  pthread_t *tids = (pthread_t *)calloc(threads, sizeof(pthread_t));
+  for(uint32_t i = 0; i < threads; i++)
+  {
+    jobs[i].s = s;
+    jobs[i].first = first;
+    jobs[i].count = count;
+    jobs[i].colors = colors;
+    jobs[i].depths = depths;
+    jobs[i].y0 = (int)((uint64_t)maxh * i / threads);
+    jobs[i].y1 = i + 1 == threads ? INT_MAX : (int)((uint64_t)maxh * (i + 1) / threads);
+    jobs[i].count_prims = i == 0;
+    pthread_create(&tids[i], NULL, band_main, &jobs[i]);
+  }
+  vor_counters tot;
+  memset(&tot, 0, sizeof(tot));
+  for(uint32_t i = 0; i < threads; i++)
+  {
+    pthread_join(tids[i], NULL);
+    tot.tris_in += jobs[i].cnt.tris_in;
+    tot.tris_out += jobs[i].cnt.tris_out;
+    tot.tested += jobs[i].cnt.tested;
+    tot.covered += jobs[i].cnt.covered;
+    tot.shaded += jobs[i].cnt.shaded;
+    tot.draws += jobs[i].cnt.draws;
+  }
+  if(counters)
+    *counters = tot;
+  free(jobs);
+  free(tids);
+  return 0;
 }

@@ -45,6 +45,11 @@ int vor_render(const vsc_scene *scene, uint8_t **colors, float **depths, vor_cou
 int vor_render_passes(const vsc_scene *scene, uint32_t first, uint32_t count, uint8_t **colors,
                       float **depths, vor_counters *counters);
 
+/* Multi-threaded CPU baseline: horizontal bands rendered by `threads` workers
+   (same output as vor_render_passes). */
+int vor_render_threads(const vsc_scene *scene, uint32_t first, uint32_t count, uint8_t **colors,
+                       float **depths, vor_counters *counters, uint32_t threads);
+
 /* Texture sampling entry points, exposed for unit tests. */
 void vor_sample_bilinear(const uint8_t *texels, uint32_t width, uint32_t height, float u, float v,
                          float out[4]);

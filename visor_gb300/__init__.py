@@ -39,7 +39,8 @@ class VgpuStats(C.Structure):
 
 
 class VgpuTuning(C.Structure):
-    _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("use_graphs", C.c_uint32)]
+    _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("use_graphs", C.c_uint32),
+                ("time_raster", C.c_uint32)]
 
 
 def lib():
@@ -87,6 +88,10 @@ def lib():
                                      C.POINTER(C.c_uint64)]
     L.vgpu_program_check.restype = C.c_int
     L.vgpu_set_tuning.argtypes = [C.POINTER(VgpuTuning)]
+    L.vgpu_queue_flush_l2.argtypes = [VP]
+    L.vgpu_queue_flush_l2.restype = C.c_int
+    L.visor_gb300_flush_l2.argtypes = [VP]
+    L.visor_gb300_flush_l2.restype = C.c_int
     L.vgpu_get_tuning.argtypes = [C.POINTER(VgpuTuning)]
     _lib = L
     return L
@@ -130,7 +135,7 @@ def set_mode(mode):
     lib().visor_gb300_set_mode(mode)
 
 
-def set_tuning(raster_blocks_per_sm=None, use_graphs=None):
+def set_tuning(raster_blocks_per_sm=None, use_graphs=None, time_raster=None):
     L = lib()
     t = VgpuTuning()
     L.vgpu_get_tuning(C.byref(t))
@@ -138,7 +143,15 @@ def set_tuning(raster_blocks_per_sm=None, use_graphs=None):
         t.raster_blocks_per_sm = raster_blocks_per_sm
     if use_graphs is not None:
         t.use_graphs = use_graphs
+    if time_raster is not None:
+        t.time_raster = time_raster
     L.vgpu_set_tuning(C.byref(t))
+
+
+def get_tuning():
+    t = VgpuTuning()
+    lib().vgpu_get_tuning(C.byref(t))
+    return {n: getattr(t, n) for n, _ in VgpuTuning._fields_}
 
 
 class Device:
@@ -167,6 +180,12 @@ class Device:
 
     def reset_stats(self):
         self.lib.visor_gb300_queue_reset_stats(self.queue)
+
+    def flush_l2(self):
+        """Overwrite 512 MiB on the queue's stream so the next step starts with a cold L2."""
+        rc = self.lib.visor_gb300_flush_l2(self.queue)
+        if rc != 0:
+            raise RuntimeError(f"L2 flush failed: {rc}")
 
     def upload(self, handle, flags=0):
         """Create every Vulkan object of a scene and record its command buffer."""

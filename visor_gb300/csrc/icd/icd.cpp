@@ -1626,6 +1626,8 @@ VISOR_EXPORT int visor_gb300_queue_stats(VkQueue q, vgpu_stats *out) { return vg
 
 VISOR_EXPORT void visor_gb300_queue_reset_stats(VkQueue q) { vgpu_queue_reset_stats(q->q); }
 
+VISOR_EXPORT int visor_gb300_flush_l2(VkQueue q) { return vgpu_queue_flush_l2(q->q); }
+
 VISOR_EXPORT size_t visor_gb300_pipeline_source(VkPipeline p, char *buf, size_t size)
 {
   const std::string &s = p->tr.source;

@@ -113,7 +113,8 @@ namespace
 std::mutex g_mu;
 bool g_init = false;
 int g_sms = 148;
-vgpu_tuning g_tuning = {2, 1};
+int g_device = 0;
+vgpu_tuning g_tuning = {2, 1, 0};
 
 /* ------------------------------------------------------------------------ */
 /* generic kernels                                                           */
@@ -389,10 +390,15 @@ extern "C" int vgpu_init(void)
     fprintf(stderr, "visor_gb300: no CUDA device available\n");
     return VGPU_ERROR_INITIALIZATION_FAILED;
   }
-  CK(cudaSetDevice(0));
+  /* one process per GPU: VISOR_GB300_DEVICE, else the launcher's LOCAL_RANK */
+  const char *dv = getenv("VISOR_GB300_DEVICE");
+  if(!dv)
+    dv = getenv("LOCAL_RANK");
+  g_device = dv ? atoi(dv) % n : 0;
+  CK(cudaSetDevice(g_device));
   CK(cudaFree(0));
   cudaDeviceProp prop;
-  CK(cudaGetDeviceProperties(&prop, 0));
+  CK(cudaGetDeviceProperties(&prop, g_device));
   g_sms = prop.multiProcessorCount;
   int rc = load_driver_api();
   if(rc)
@@ -407,7 +413,7 @@ extern "C" int vgpu_device_info_get(vgpu_device_info *out)
   if(rc)
     return rc;
   cudaDeviceProp prop;
-  CK(cudaGetDeviceProperties(&prop, 0));
+  CK(cudaGetDeviceProperties(&prop, g_device));
   memset(out, 0, sizeof(*out));
   snprintf(out->name, sizeof(out->name), "%s", prop.name);
   out->total_memory = prop.totalGlobalMem;
@@ -422,6 +428,7 @@ extern "C" int vgpu_mem_alloc(uint64_t bytes, int host_visible, void **dptr, voi
   int rc = vgpu_init();
   if(rc)
     return rc;
+  CK(cudaSetDevice(g_device));
   *dptr = nullptr;
   if(hptr)
     *hptr = nullptr;
@@ -531,6 +538,7 @@ extern "C" int vgpu_program_create(const char *shader_source, uint32_t tile_shif
   static std::map<u64, std::vector<char>> mem_cache;
   const u64 h = hash_str(src + "|sm_103a|fmad=false");
   std::vector<char> cubin;
+  CK(cudaSetDevice(g_device));
   {
     std::lock_guard<std::mutex> lk(g_mu);
     auto it = mem_cache.find(h);
@@ -577,7 +585,6 @@ extern "C" int vgpu_program_create(const char *shader_source, uint32_t tile_shif
   p->k = k;
   p->tile_shift = tile_shift;
   p->rec_words = ((20 + 3 * k) + 3) & ~3u;
-  CK(cudaSetDevice(0));
   CU(g_cu.moduleLoadData(&p->mod, cubin.data()));
   CU(g_cu.moduleGetFunction(&p->setup, p->mod, "vgx_setup"));
   CU(g_cu.moduleGetFunction(&p->raster, p->mod, "vgx_raster"));
@@ -920,6 +927,9 @@ struct vgpu_queue
   u32 *status = nullptr;  /* 4 words per job slot */
   u64 *counters = nullptr; /* tris_out, tested, covered, shaded */
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> rev; /* raster start/stop pairs of the last submit */
+  size_t rev_used = 0;
+  u32 *flush = nullptr;         /* L2 flush buffer */
   vgpu_stats stats;
   u64 launches = 0;
   bool timed = false;
@@ -938,6 +948,7 @@ extern "C" int vgpu_queue_create(vgpu_queue **out)
   if(rc)
     return rc;
   vgpu_queue *q = new vgpu_queue();
+  CK(cudaSetDevice(g_device));
   CK(cudaStreamCreateWithFlags(&q->stream, cudaStreamNonBlocking));
   CK(cudaMalloc(&q->status, 64));
   CK(cudaMemset(q->status, 0, 64));
@@ -969,6 +980,9 @@ extern "C" void vgpu_queue_destroy(vgpu_queue *q)
   cudaFree(q->counters);
   cudaEventDestroy(q->ev0);
   cudaEventDestroy(q->ev1);
+  for(cudaEvent_t e : q->rev)
+    cudaEventDestroy(e);
+  cudaFree(q->flush);
   cudaStreamDestroy(q->stream);
   delete q;
 }
@@ -1169,7 +1183,23 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
   const unsigned warps = j.prog->rec_words > 40 ? 4 : 8; /* VGX_RASTER_WARPS */
   grid = std::min<unsigned>(grid, (warps_needed + warps - 1) / warps);
   grid = std::max(grid, 1u);
-  return launch(q, j.prog->raster, grid, warps * 32, &J);
+  if(g_tuning.time_raster)
+  {
+    while(q->rev.size() < q->rev_used + 2)
+    {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      q->rev.push_back(e);
+    }
+    CK(cudaEventRecord(q->rev[q->rev_used], q->stream));
+  }
+  int rc2 = launch(q, j.prog->raster, grid, warps * 32, &J);
+  if(g_tuning.time_raster)
+  {
+    CK(cudaEventRecord(q->rev[q->rev_used + 1], q->stream));
+    q->rev_used += 2;
+  }
+  return rc2;
 }
 
 extern "C" int vgpu_submit(vgpu_queue *q, vgpu_list *l)
@@ -1180,6 +1210,7 @@ extern "C" int vgpu_submit(vgpu_queue *q, vgpu_list *l)
     if(rc)
       return rc;
   }
+  q->rev_used = 0;
   CK(cudaEventRecord(q->ev0, q->stream));
   for(auto &u : l->uploads)
     CK(cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, q->stream));
@@ -1341,6 +1372,10 @@ extern "C" int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out)
   float ms = 0.0f;
   if(q->timed && cudaEventElapsedTime(&ms, q->ev0, q->ev1) == cudaSuccess)
     out->gpu_ms = ms;
+  out->raster_ms = 0.0;
+  for(size_t i = 0; i + 1 < q->rev_used; i += 2)
+    if(cudaEventElapsedTime(&ms, q->rev[i], q->rev[i + 1]) == cudaSuccess)
+      out->raster_ms += ms;
   return VGPU_OK;
 }
 
@@ -1355,3 +1390,13 @@ extern "C" void vgpu_queue_reset_stats(vgpu_queue *q)
 
 extern "C" void vgpu_set_tuning(const vgpu_tuning *t) { g_tuning = *t; }
 extern "C" void vgpu_get_tuning(vgpu_tuning *t) { *t = g_tuning; }
+
+/* Overwrite a buffer larger than L2 on the queue's stream (benchmark hygiene). */
+extern "C" int vgpu_queue_flush_l2(vgpu_queue *q)
+{
+  const size_t bytes = 512ull << 20;
+  if(!q->flush)
+    CK(cudaMalloc(&q->flush, bytes));
+  CK(cudaMemsetAsync(q->flush, (int)(q->launches & 0xff), bytes, q->stream));
+  return VGPU_OK;
+}
