@@ -314,9 +314,52 @@ __device__ __forceinline__ float vgx_pixdepth(const u32 *r, int b0, int b1, int 
          n[2] * __uint_as_float(r[R_DEPTH + 2]);
 }
 
-extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(VgxJob job)
+/* shared-memory layout of one batch slot: the triangle's edge planes at the
+   tile origin, so every pixel test is three integer multiply-adds */
+#define P_E 0      /* e0, e1, e2 at the tile origin; [3] state */
+#define P_STATE 3
+#define P_A 4      /* x increments; [7] invarea */
+#define P_INVAREA 7
+#define P_B 8      /* y increments; [11] draw */
+#define P_DRAW 11
+#define P_D 12     /* vertex depths z/w; [15] lod */
+#define P_LOD 15
+#define P_INVW 16  /* 1/w per vertex */
+#define P_IV 20    /* interpolants, 3 x VGX_K */
+
+/* 32x32 bit-matrix transpose across the warp: lane t holds row t on entry,
+   column t (bit r = bit t of row r) on exit. */
+__device__ __forceinline__ u32 vgx_transpose32(u32 x, int lane)
 {
-  __shared__ __align__(16) u32 s_rec[VGX_RASTER_WARPS][32][VGX_REC];
+#pragma unroll
+  for(int j = 16; j > 0; j >>= 1)
+  {
+    const u32 lo = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu
+                   : j == 2 ? 0x33333333u : 0x55555555u;
+    const u32 y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~lo) | ((y >> j) & lo)) : ((x & lo) | ((y << j) & ~lo));
+  }
+  return x;
+}
+
+__device__ __forceinline__ int vgx_edge(const u32 *s, int k, int dx, int dy)
+{
+  return (int)s[P_E + k] + (int)s[P_A + k] * dx + (int)s[P_B + k] * dy;
+}
+
+__device__ __forceinline__ float vgx_plane_depth(const u32 *s, int b0, int b1, int b2, float *n)
+{
+  const float invarea = __uint_as_float(s[P_INVAREA]);
+  n[0] = (float)b0 * invarea;
+  n[1] = (float)b1 * invarea;
+  n[2] = (float)b2 * invarea;
+  return n[0] * __uint_as_float(s[P_D]) + n[1] * __uint_as_float(s[P_D + 1]) +
+         n[2] * __uint_as_float(s[P_D + 2]);
+}
+
+extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32, 32 / VGX_RASTER_WARPS) vgx_raster(VgxJob job)
+{
+  __shared__ __align__(16) u32 s_tri[VGX_RASTER_WARPS][32][VGX_REC];
   __shared__ float4 s_col[VGX_RASTER_WARPS][32];
   __shared__ u32 s_pass[VGX_RASTER_WARPS][32][2];
   __shared__ u32 s_off[VGX_RASTER_WARPS][32];
@@ -332,8 +375,9 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
   const u32 *vals = (const u32 *)job.vals;
   const u32 *tstart = (const u32 *)job.tile_start, *tend = (const u32 *)job.tile_end;
   const u32 nwork = job.all_tiles ? job.num_tiles : status[3];
-  u32(*rec)[VGX_REC] = s_rec[wib];
+  u32(*tri)[VGX_REC] = s_tri[wib];
   u64 covered_total = 0, shaded_total = 0;
+  const int ldx = lane & 7, ldy = lane >> 3;
 
   for(;;)
   {
@@ -345,7 +389,6 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
       break;
     const u32 tile = job.work ? ((const u32 *)job.work)[w] : w;
 
-    /* target of this tile */
     u32 lo = 0, hi = job.num_targets - 1;
     while(lo < hi)
     {
@@ -357,11 +400,11 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
     }
     const VgxTarget T = targets[lo];
     const u32 local = tile - T.tile_base;
-    const int tx = (int)(local % T.tiles_x), ty = (int)(local / T.tiles_x);
-    const int px = (tx << VGX_TILE_SHIFT) + (lane & (VGX_TILE - 1));
+    const int x0 = (int)(local % T.tiles_x) << 3, y0 = (int)(local / T.tiles_x) << 3;
+    const int px = x0 + ldx;
     int py[2];
-    py[0] = (ty << VGX_TILE_SHIFT) + (lane >> VGX_TILE_SHIFT);
-    py[1] = py[0] + (32 >> VGX_TILE_SHIFT);
+    py[0] = y0 + ldy;
+    py[1] = py[0] + 4;
     bool in[2];
     u32 col[2];
     float dep[2];
@@ -388,26 +431,130 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
     for(u32 base = start; base < end; base += 32)
     {
       const u32 n = min(32u, end - base);
+      /* lane t: its triangle's planes, coverage mask over the 8x8 tile, depth bounds */
+      u32 mlo = 0, mhi = 0, st = 0;
+      float dlo = 0.0f, dhi = 0.0f;
+      bool finite = false;
       if((u32)lane < n)
       {
         const u32 t = vals[base + lane];
-        const uint4 *src = (const uint4 *)((const u32 *)job.records + (u64)t * VGX_REC);
-        uint4 *dst = (uint4 *)rec[lane];
+        const u32 *g = (const u32 *)job.records + (u64)t * VGX_REC;
+        int r[VGX_REC_HEAD];
 #pragma unroll
-        for(int q = 0; q < VGX_REC / 4; q++)
-          dst[q] = __ldg(src + q);
+        for(int q = 0; q < VGX_REC_HEAD; q += 4)
+        {
+          uint4 v = __ldg((const uint4 *)(g + q));
+          r[q] = (int)v.x;
+          r[q + 1] = (int)v.y;
+          r[q + 2] = (int)v.z;
+          r[q + 3] = (int)v.w;
+        }
+        const int v0x = r[R_V0X], v0y = r[R_V0Y], ABx = r[R_ABX], ABy = r[R_ABY];
+        const int ACx = r[R_ACX], ACy = r[R_ACY], bm = r[R_BARYMUL];
+        /* barycentric (rasterizer.cpp:303-309) expanded into affine planes in (x, y);
+           every product and sum is exact modulo 2^32, so each pixel's value equals the
+           reference's direct evaluation */
+        const int c1 = ACx * v0y - ACy * v0x, c2 = v0x * ABy - v0y * ABx;
+        const int a1 = bm * ACy, b1 = -(bm * ACx), a2 = -(bm * ABy), b2 = bm * ABx;
+        const int a0 = -(a1 + a2), b0 = -(b1 + b2);
+        const int e1 = a1 * x0 + b1 * y0 + bm * c1;
+        const int e2 = a2 * x0 + b2 * y0 + bm * c2;
+        const int e0 = a0 * x0 + b0 * y0 + bm * (r[R_AREA2] - c1 - c2);
+        st = (u32)r[R_STATE];
+        u32 *s = tri[lane];
+        *(uint4 *)(s + P_E) = make_uint4((u32)e0, (u32)e1, (u32)e2, st);
+        *(uint4 *)(s + P_A) = make_uint4((u32)a0, (u32)a1, (u32)a2, (u32)r[R_INVAREA]);
+        *(uint4 *)(s + P_B) = make_uint4((u32)b0, (u32)b1, (u32)b2, (u32)r[R_DRAW]);
+        *(uint4 *)(s + P_D) = make_uint4((u32)r[R_DEPTH], (u32)r[R_DEPTH + 1], (u32)r[R_DEPTH + 2],
+                                         (u32)r[R_LOD]);
+        *(uint4 *)(s + P_INVW) = make_uint4((u32)r[R_INVW], (u32)r[R_INVW + 1], (u32)r[R_INVW + 2], 0u);
+#pragma unroll
+        for(int q = VGX_REC_HEAD; q < VGX_REC; q += 4)
+          *(uint4 *)(s + q) = __ldg((const uint4 *)(g + q));
+        /* coverage of the tile, clipped to the bbox [min, max) (rasterizer.cpp:538-549) */
+        const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
+        const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
+        const int cx0 = max(minx - x0, 0), cx1 = min(maxx - x0, 8);
+        const int ry0 = max(miny - y0, 0), ry1 = min(maxy - y0, 8);
+        if(cx0 < cx1 && ry0 < ry1)
+        {
+          const u32 colmask = (0xffu >> (8 - cx1)) & (0xffu << cx0);
+          for(int dy = ry0; dy < ry1; dy++)
+          {
+            int q0 = e0 + b0 * dy, q1 = e1 + b1 * dy, q2 = e2 + b2 * dy;
+            u32 row = 0;
+#pragma unroll
+            for(int dx = 0; dx < 8; dx++)
+            {
+              row |= ((u32)(~(q0 | q1 | q2)) >> 31) << dx;
+              q0 += a0;
+              q1 += a1;
+              q2 += a2;
+            }
+            row &= colmask;
+            if(dy < 4)
+              mlo |= row << (dy * 8);
+            else
+              mhi |= row << ((dy - 4) * 8);
+          }
+        }
+        const float d0 = __int_as_float(r[R_DEPTH]), d1 = __int_as_float(r[R_DEPTH + 1]),
+                    d2 = __int_as_float(r[R_DEPTH + 2]);
+        finite = isfinite(d0) && isfinite(d1) && isfinite(d2);
+        const float mag = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
+        const float margin = mag * 2.0e-6f + 1.0e-30f; /* > the rounding of pixdepth (~4e-7 relative) */
+        dlo = fminf(d0, fminf(d1, d2)) - margin;
+        dhi = fmaxf(d0, fmaxf(d1, d2)) + margin;
       }
+      covered_total += __popc(mlo) + __popc(mhi);
+
+      /* conservative depth rejection of whole triangles against the tile's depth range */
+      float tmax = __int_as_float(0xff800000), tmin = __int_as_float(0x7f800000);
+#pragma unroll
+      for(int p = 0; p < 2; p++)
+        if(in[p])
+        {
+          tmax = fmaxf(tmax, dep[p]);
+          tmin = fminf(tmin, dep[p]);
+        }
+#pragma unroll
+      for(int o = 16; o > 0; o >>= 1)
+      {
+        tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+        tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
+      }
+      const bool has = (mlo | mhi) != 0;
+      const u32 op = S_DEPTH_OP(st);
+      const bool writes = has && (st & S_DEPTH_WRITE);
+      const bool tested = (st & S_DEPTH_TEST) != 0;
+      /* can any triangle of this batch raise (lower) a stored depth? */
+      const bool raises = writes && !(tested && op <= 3u);
+      const bool lowers = writes && !(tested && (op == 0u || op == 2u || op == 4u || op == 6u));
+      const bool any_raise = __any_sync(0xffffffffu, raises);
+      const bool any_lower = __any_sync(0xffffffffu, lowers);
+      bool skip = false;
+      if(has && tested)
+      {
+        if(op == 0u)
+          skip = true;
+        else if(finite && !any_raise && ((op == 1u && dlo >= tmax) || (op == 3u && dlo > tmax)))
+          skip = true;
+        else if(finite && !any_lower && ((op == 4u && dhi <= tmin) || (op == 6u && dhi < tmin)))
+          skip = true;
+        else if(finite && !any_raise && !any_lower && op == 2u && (dlo > tmax || dhi < tmin))
+          skip = true;
+      }
+      const u32 live = __ballot_sync(0xffffffffu, has && !skip);
       __syncwarp();
 
-      /* coverage words: bit t set when triangle t of the batch covers the pixel */
-      u32 cov[2] = {0u, 0u};
-      for(u32 t = 0; t < n; t++)
-      {
-#pragma unroll
-        for(int p = 0; p < 2; p++)
-          if(in[p] && vgx_covers(rec[t], px, py[p]))
-            cov[p] |= 1u << t;
-      }
+      /* per-pixel coverage words: bit t set when triangle t covers the pixel */
+      u32 cov[2];
+      cov[0] = vgx_transpose32(mlo, lane) & live;
+      cov[1] = vgx_transpose32(mhi, lane) & live;
+      if(!in[0])
+        cov[0] = 0;
+      if(!in[1])
+        cov[1] = 0;
 
       /* early depth test in primitive order per pixel */
       u32 pass[2] = {0u, 0u};
@@ -415,28 +562,27 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
       for(int p = 0; p < 2; p++)
       {
         u32 m = cov[p];
+        const int dy = ldy + 4 * p;
         while(m)
         {
           const u32 t = __ffs(m) - 1;
           m &= m - 1;
-          const u32 *r = rec[t];
-          const u32 st = r[R_STATE];
-          int b0, b1, b2;
-          vgx_bary(r, px, py[p], b0, b1, b2);
+          const u32 *s = tri[t];
+          const u32 stt = s[P_STATE];
           float nn[3];
-          const float z = vgx_pixdepth(r, b0, b1, b2, nn);
+          const float z = vgx_plane_depth(s, vgx_edge(s, 0, ldx, dy), vgx_edge(s, 1, ldx, dy),
+                                          vgx_edge(s, 2, ldx, dy), nn);
           bool ok = true;
-          if(st & S_DEPTH_TEST)
-            ok = vgx_depth_pass(S_DEPTH_OP(st), z, dep[p]);
+          if(stt & S_DEPTH_TEST)
+            ok = vgx_depth_pass(S_DEPTH_OP(stt), z, dep[p]);
           if(ok)
           {
             pass[p] |= 1u << t;
-            if(st & S_DEPTH_WRITE)
+            if(stt & S_DEPTH_WRITE)
               dep[p] = z;
           }
         }
       }
-      covered_total += __popc(cov[0]) + __popc(cov[1]);
       const u32 mine = __popc(pass[0]) + __popc(pass[1]);
       shaded_total += mine;
 
@@ -461,7 +607,6 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
         const u32 f = chunk + lane;
         if(f < total)
         {
-          /* owner lane: last lane whose exclusive offset <= f */
           u32 olo = 0, ohi = 31;
           while(olo < ohi)
           {
@@ -471,7 +616,7 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
             else
               ohi = mid - 1;
           }
-          u32 k = f - s_off[wib][olo];
+          const u32 k = f - s_off[wib][olo];
           const u32 p0 = s_pass[wib][olo][0];
           const u32 c0 = __popc(p0);
           const int sel = k < c0 ? 0 : 1;
@@ -480,32 +625,30 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
           while(kk--)
             m &= m - 1;
           const u32 t = __ffs(m) - 1;
-          const int fx = (int)(olo & (VGX_TILE - 1)) + (tx << VGX_TILE_SHIFT);
-          const int fy = (ty << VGX_TILE_SHIFT) + (int)(olo >> VGX_TILE_SHIFT) + sel * (32 >> VGX_TILE_SHIFT);
-          const u32 *r = rec[t];
-          int b0, b1, b2;
-          vgx_bary(r, fx, fy, b0, b1, b2);
+          const int fdx = (int)(olo & 7), fdy = (int)(olo >> 3) + 4 * sel;
+          const u32 *s = tri[t];
           float nb[4];
-          (void)vgx_pixdepth(r, b0, b1, b2, nb);
+          (void)vgx_plane_depth(s, vgx_edge(s, 0, fdx, fdy), vgx_edge(s, 1, fdx, fdy),
+                                vgx_edge(s, 2, fdx, fdy), nb);
           /* perspective correction, rasterizer.cpp:580-588 */
-          nb[0] = nb[0] * __uint_as_float(r[R_INVW]);
-          nb[1] = nb[1] * __uint_as_float(r[R_INVW + 1]);
-          nb[2] = nb[2] * __uint_as_float(r[R_INVW + 2]);
+          nb[0] = nb[0] * __uint_as_float(s[P_INVW]);
+          nb[1] = nb[1] * __uint_as_float(s[P_INVW + 1]);
+          nb[2] = nb[2] * __uint_as_float(s[P_INVW + 2]);
           const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
           nb[0] = nb[0] * invlen;
           nb[1] = nb[1] * invlen;
           nb[2] = nb[2] * invlen;
           nb[3] = 0.0f;
-          const float *iv = (const float *)(r + VGX_REC_HEAD);
-          s_col[wib][lane] = vgx_fs(draws[r[R_DRAW]], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
-                                    __uint_as_float(r[R_LOD]));
+          const float *iv = (const float *)(s + P_IV);
+          s_col[wib][lane] = vgx_fs(draws[s[P_DRAW]], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
+                                    __uint_as_float(s[P_LOD]));
         }
         __syncwarp();
         /* in-order blend: each owner consumes its fragments of this chunk */
         const u32 lo_f = max(excl, chunk), hi_f = min(excl + mine, chunk + 32);
         for(u32 g = lo_f; g < hi_f; g++)
         {
-          u32 k = g - excl;
+          const u32 k = g - excl;
           const u32 c0 = __popc(pass[0]);
           const int sel = k < c0 ? 0 : 1;
           u32 m = sel ? pass[1] : pass[0];
@@ -514,11 +657,11 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
             m &= m - 1;
           const u32 t = __ffs(m) - 1;
           const float4 c = s_col[wib][g - chunk];
-          const u32 st = rec[t][R_STATE];
+          const u32 stt = tri[t][P_STATE];
           if(sel == 0)
-            col[0] = vgx_blend_write(st, c, col[0]);
+            col[0] = vgx_blend_write(stt, c, col[0]);
           else
-            col[1] = vgx_blend_write(st, c, col[1]);
+            col[1] = vgx_blend_write(stt, c, col[1]);
         }
         __syncwarp();
       }

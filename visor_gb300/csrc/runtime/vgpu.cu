@@ -114,7 +114,7 @@ std::mutex g_mu;
 bool g_init = false;
 int g_sms = 148;
 int g_device = 0;
-vgpu_tuning g_tuning = {2, 1, 0};
+vgpu_tuning g_tuning = {4, 1, 0};
 
 /* ------------------------------------------------------------------------ */
 /* generic kernels                                                           */
@@ -478,10 +478,20 @@ static int compile_cubin(const std::string &src, std::vector<char> &cubin, char 
     return VGPU_ERROR_INITIALIZATION_FAILED;
   const char *opts[] = {"--gpu-architecture=sm_103a", "--fmad=false", "--prec-div=true",
                         "--prec-sqrt=true", "--ftz=false", "-default-device", "--std=c++17",
-                        "-lineinfo"};
-  nvrtcResult r = nvrtcCompileProgram(prog, sizeof(opts) / sizeof(opts[0]), opts);
+                        "-lineinfo", "-diag-suppress=177"};
+  std::vector<const char *> ov(opts, opts + sizeof(opts) / sizeof(opts[0]));
+  const bool verbose = getenv("VISOR_GB300_PTXAS_VERBOSE") != nullptr;
+  if(verbose)
+    ov.push_back("--ptxas-options=-v");
+  nvrtcResult r = nvrtcCompileProgram(prog, (int)ov.size(), ov.data());
   size_t ls = 0;
   nvrtcGetProgramLogSize(prog, &ls);
+  if(verbose && r == NVRTC_SUCCESS)
+  {
+    std::string l(ls, '\0');
+    nvrtcGetProgramLog(prog, &l[0]);
+    fprintf(stderr, "%s\n", l.c_str());
+  }
   if(r != NVRTC_SUCCESS)
   {
     std::string l(ls, '\0');
@@ -1134,6 +1144,7 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
     CK(cudaMemsetAsync(q->tstart, 0, (size_t)j.num_tiles * 4, q->stream));
     CK(cudaMemsetAsync(q->tend, 0, (size_t)j.num_tiles * 4, q->stream));
   }
+  q->stats.pairs += total;
   if(total)
   {
     k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.prog->rec_words, counts);
