@@ -214,6 +214,14 @@ def run_ours(args):
     w, hgt = h.targets()[0]
     tris = h.triangle_count()
 
+    # autotune bin tile and warps per bin on this workload (outside the timed region)
+    from visor_gb300 import tune
+    if args.bin_shift:
+        choice, tuned = (args.bin_shift, args.warps), {}
+        vg.set_tuning(bin_shift=args.bin_shift, raster_warps=args.warps)
+    else:
+        choice, tuned = tune.tune(dev, h, vg.DEVICE_TARGETS)
+
     results = {}
     modes = [("batched", vg.MODE_BATCHED)]
     if not args.only_batched:
@@ -287,6 +295,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "seed": SEED, "width": w, "height": hgt, "triangles": tris,
                    "mode": "batched", "l2": "flushed between steps (512 MiB write)",
+                   "bin_tile": 1 << choice[0], "warps_per_bin": choice[1],
+                   "autotune_ms": {f"{1 << k[0]}x{1 << k[0]}/{k[1]}w": round(v, 4) for k, v in tuned.items()},
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "mtris_per_s": world * tris / (ms / 1e3) / 1e6,
         "covered_gfrags_per_s": world * b["covered"] / (ms / 1e3) / 1e9,
@@ -331,6 +341,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--triangles", type=int, default=0,
                     help="smaller triangle count of the same workload (profiling captures)")
+    ap.add_argument("--bin-shift", type=int, default=0, help="fix the bin tile (log2 edge) instead of autotuning")
+    ap.add_argument("--warps", type=int, default=1, help="warps per bin when --bin-shift is given")
     ap.add_argument("--only-batched", action="store_true",
                     help="time only the batched device-resident path (profiling captures)")
     args = ap.parse_args()

@@ -65,3 +65,23 @@ def test_gpu_matches_oracle(device, oracle, name, mode):
     ref = GOLDEN.get(name) or SPEC.get(name)
     assert _digest(gc, gd) == ref["targets"]
     assert gk == ref["counters"]
+
+
+VARIANT_SCENES = ["blend_overlap", "depth_lequal", "offscreen", "strip", "texture_wrap", "load_pass",
+                  "cfg1_sphere", "cfg2_small_blend", "cfg3_small_trilinear", "cfg4_small"]
+
+
+@pytest.mark.parametrize("variant", [(4, 1), (4, 4), (5, 8), (5, 16), (6, 16)])
+@pytest.mark.parametrize("name", VARIANT_SCENES)
+def test_bin_variants_match_oracle(device, oracle, name, variant):
+    """Every bin tile / warps-per-bin configuration the autotuner may pick renders identically."""
+    vg.set_tuning(bin_shift=variant[0], raster_warps=variant[1])
+    try:
+        h = scenes_edge.build(vg.lib(), name)
+        gc, gd, gk = vg.render(h, vg.MODE_BATCHED, device)
+    finally:
+        vg.set_tuning(bin_shift=3, raster_warps=1)
+    ho = scenes_edge.build(oracle.lib, name)
+    oc, od, ok = oracle.render(ho)
+    _compare(gc, gd, oc, od)
+    assert gk == ok

@@ -40,7 +40,7 @@ class VgpuStats(C.Structure):
 
 class VgpuTuning(C.Structure):
     _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("use_graphs", C.c_uint32),
-                ("time_raster", C.c_uint32)]
+                ("time_raster", C.c_uint32), ("bin_shift", C.c_uint32), ("raster_warps", C.c_uint32)]
 
 
 def lib():
@@ -120,12 +120,12 @@ def translate(vs_words, fs_words):
     return out.value.decode()
 
 
-def nvrtc_check(source, tile_shift=3):
+def nvrtc_check(source, tile_shift=3, warps=1):
     """NVRTC-compile translated source with the stage kernels for sm_103a; returns cubin bytes."""
     L = lib()
     log = C.create_string_buffer(65536)
     nbytes = C.c_uint64(0)
-    rc = L.vgpu_program_check(source.encode(), tile_shift, log, 65536, C.byref(nbytes))
+    rc = L.vgpu_program_check(source.encode(), tile_shift | (warps << 8), log, 65536, C.byref(nbytes))
     if rc != 0:
         raise RuntimeError("NVRTC failed:\n" + log.value.decode())
     return int(nbytes.value)
@@ -135,10 +135,16 @@ def set_mode(mode):
     lib().visor_gb300_set_mode(mode)
 
 
-def set_tuning(raster_blocks_per_sm=None, use_graphs=None, time_raster=None):
+def set_tuning(raster_blocks_per_sm=None, use_graphs=None, time_raster=None, bin_shift=None,
+               raster_warps=None):
+    """Runtime knobs read when a command buffer is lowered (autotuned by visor_gb300.tune)."""
     L = lib()
     t = VgpuTuning()
     L.vgpu_get_tuning(C.byref(t))
+    if bin_shift is not None:
+        t.bin_shift = bin_shift
+    if raster_warps is not None:
+        t.raster_warps = raster_warps
     if raster_blocks_per_sm is not None:
         t.raster_blocks_per_sm = raster_blocks_per_sm
     if use_graphs is not None:

@@ -29,8 +29,14 @@
 #endif
 #define VGX_TILE (1 << VGX_TILE_SHIFT)
 #define VGX_REC (((VGX_REC_HEAD + 3 * VGX_K) + 3) & ~3)
-/* 8 warps per CTA while the per-warp record batch fits static shared memory */
-#define VGX_RASTER_WARPS (VGX_REC > 40 ? 4 : 8)
+/* warps per raster CTA; a CTA owns one bin tile of 2^VGX_TILE_SHIFT pixels and
+   its warps split it into 8x8 sub-tiles */
+#ifndef VGX_RASTER_WARPS
+#define VGX_RASTER_WARPS 1
+#endif
+#define VGX_SUB_EDGE (1 << (VGX_TILE_SHIFT - 3))
+#define VGX_SUBS (VGX_SUB_EDGE * VGX_SUB_EDGE)
+#define VGX_SUBS_PER_WARP ((VGX_SUBS + VGX_RASTER_WARPS - 1) / VGX_RASTER_WARPS)
 
 /* state word */
 #define S_DEPTH_OP(s) ((s)&7u)
@@ -314,19 +320,6 @@ __device__ __forceinline__ float vgx_pixdepth(const u32 *r, int b0, int b1, int 
          n[2] * __uint_as_float(r[R_DEPTH + 2]);
 }
 
-/* shared-memory layout of one batch slot: the triangle's edge planes at the
-   tile origin, so every pixel test is three integer multiply-adds */
-#define P_E 0      /* e0, e1, e2 at the tile origin; [3] state */
-#define P_STATE 3
-#define P_A 4      /* x increments; [7] invarea */
-#define P_INVAREA 7
-#define P_B 8      /* y increments; [11] draw */
-#define P_DRAW 11
-#define P_D 12     /* vertex depths z/w; [15] lod */
-#define P_LOD 15
-#define P_INVW 16  /* 1/w per vertex */
-#define P_IV 20    /* interpolants, 3 x VGX_K */
-
 /* 32x32 bit-matrix transpose across the warp: lane t holds row t on entry,
    column t (bit r = bit t of row r) on exit. */
 __device__ __forceinline__ u32 vgx_transpose32(u32 x, int lane)
@@ -342,27 +335,286 @@ __device__ __forceinline__ u32 vgx_transpose32(u32 x, int lane)
   return x;
 }
 
-__device__ __forceinline__ int vgx_edge(const u32 *s, int k, int dx, int dy)
+/* per-warp plane of a batch triangle at the warp's sub-tile origin:
+   [0] e0 e1 e2 state, [1] x increments + invarea bits, [2] y increments + draw */
+struct VgxPlane
 {
-  return (int)s[P_E + k] + (int)s[P_A + k] * dx + (int)s[P_B + k] * dy;
+  uint4 e, a, b;
+};
+
+__device__ __forceinline__ int vgx_edge(const VgxPlane &p, int k, int dx, int dy)
+{
+  const u32 e = k == 0 ? p.e.x : k == 1 ? p.e.y : p.e.z;
+  const u32 a = k == 0 ? p.a.x : k == 1 ? p.a.y : p.a.z;
+  const u32 b = k == 0 ? p.b.x : k == 1 ? p.b.y : p.b.z;
+  return (int)e + (int)a * dx + (int)b * dy;
 }
 
-__device__ __forceinline__ float vgx_plane_depth(const u32 *s, int b0, int b1, int b2, float *n)
+__device__ __forceinline__ float vgx_plane_depth(const VgxPlane &p, const u32 *raw, int dx, int dy,
+                                                 float *n)
 {
-  const float invarea = __uint_as_float(s[P_INVAREA]);
-  n[0] = (float)b0 * invarea;
-  n[1] = (float)b1 * invarea;
-  n[2] = (float)b2 * invarea;
-  return n[0] * __uint_as_float(s[P_D]) + n[1] * __uint_as_float(s[P_D + 1]) +
-         n[2] * __uint_as_float(s[P_D + 2]);
+  const float invarea = __uint_as_float(p.a.w);
+  n[0] = (float)vgx_edge(p, 0, dx, dy) * invarea;
+  n[1] = (float)vgx_edge(p, 1, dx, dy) * invarea;
+  n[2] = (float)vgx_edge(p, 2, dx, dy) * invarea;
+  return n[0] * __uint_as_float(raw[R_DEPTH]) + n[1] * __uint_as_float(raw[R_DEPTH + 1]) +
+         n[2] * __uint_as_float(raw[R_DEPTH + 2]);
 }
 
-extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32, 32 / VGX_RASTER_WARPS) vgx_raster(VgxJob job)
+struct VgxRasterShared
 {
-  __shared__ __align__(16) u32 s_tri[VGX_RASTER_WARPS][32][VGX_REC];
-  __shared__ float4 s_col[VGX_RASTER_WARPS][32];
-  __shared__ u32 s_pass[VGX_RASTER_WARPS][32][2];
-  __shared__ u32 s_off[VGX_RASTER_WARPS][32];
+  u32 raw[32][VGX_REC] __attribute__((aligned(16))); /* the batch's records, shared by the CTA */
+  VgxPlane plane[VGX_RASTER_WARPS][32];
+  float4 col[VGX_RASTER_WARPS][32];
+  u32 pass[VGX_RASTER_WARPS][32][2];
+  u32 off[VGX_RASTER_WARPS][32];
+  u32 bin;
+};
+
+/*
+ * One warp, one 8x8 sub-tile at (x0, y0), one batch of n <= 32 triangles
+ * already in shared memory.  Lane L owns pixels (L&7, L>>3) and (L&7, (L>>3)+4);
+ * their colour and depth live in col[]/dep[] for the whole bin.
+ */
+__device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterShared &sh, int wib,
+                                                  int lane, u32 n, int x0, int y0, const bool *in,
+                                                  u32 *col, float *dep, u64 &covered_total,
+                                                  u64 &shaded_total)
+{
+  const VgxDraw *draws = (const VgxDraw *)job.draws;
+  const int ldx = lane & 7, ldy = lane >> 3;
+  VgxPlane *pl = sh.plane[wib];
+
+  /* lane t: its triangle's planes at the sub-tile origin, coverage mask, depth bounds */
+  u32 mlo = 0, mhi = 0, st = 0;
+  float dlo = 0.0f, dhi = 0.0f;
+  bool finite = false;
+  if((u32)lane < n)
+  {
+    const u32 *r = sh.raw[lane];
+    const int v0x = (int)r[R_V0X], v0y = (int)r[R_V0Y], ABx = (int)r[R_ABX], ABy = (int)r[R_ABY];
+    const int ACx = (int)r[R_ACX], ACy = (int)r[R_ACY], bm = (int)r[R_BARYMUL];
+    /* barycentric (rasterizer.cpp:303-309) expanded into affine planes in (x, y);
+       every product and sum is exact modulo 2^32, so each pixel's value equals the
+       reference's direct evaluation */
+    const int c1 = ACx * v0y - ACy * v0x, c2 = v0x * ABy - v0y * ABx;
+    const int a1 = bm * ACy, b1 = -(bm * ACx), a2 = -(bm * ABy), b2 = bm * ABx;
+    const int a0 = -(a1 + a2), b0 = -(b1 + b2);
+    const int e1 = a1 * x0 + b1 * y0 + bm * c1;
+    const int e2 = a2 * x0 + b2 * y0 + bm * c2;
+    const int e0 = a0 * x0 + b0 * y0 + bm * ((int)r[R_AREA2] - c1 - c2);
+    st = r[R_STATE];
+    VgxPlane p;
+    p.e = make_uint4((u32)e0, (u32)e1, (u32)e2, st);
+    p.a = make_uint4((u32)a0, (u32)a1, (u32)a2, r[R_INVAREA]);
+    p.b = make_uint4((u32)b0, (u32)b1, (u32)b2, r[R_DRAW]);
+    pl[lane] = p;
+    /* coverage of the sub-tile, clipped to the bbox [min, max) (rasterizer.cpp:538-549) */
+    const int minx = (int)(r[R_MIN] & 0xffffu), miny = (int)(r[R_MIN] >> 16);
+    const int maxx = (int)(r[R_MAX] & 0xffffu), maxy = (int)(r[R_MAX] >> 16);
+    const int cx0 = max(minx - x0, 0), cx1 = min(maxx - x0, 8);
+    const int ry0 = max(miny - y0, 0), ry1 = min(maxy - y0, 8);
+    if(cx0 < cx1 && ry0 < ry1)
+    {
+      const u32 colmask = (0xffu >> (8 - cx1)) & (0xffu << cx0);
+      for(int dy = ry0; dy < ry1; dy++)
+      {
+        int q0 = e0 + b0 * dy, q1 = e1 + b1 * dy, q2 = e2 + b2 * dy;
+        u32 row = 0;
+#pragma unroll
+        for(int dx = 0; dx < 8; dx++)
+        {
+          row |= ((u32)(~(q0 | q1 | q2)) >> 31) << dx;
+          q0 += a0;
+          q1 += a1;
+          q2 += a2;
+        }
+        row &= colmask;
+        if(dy < 4)
+          mlo |= row << (dy * 8);
+        else
+          mhi |= row << ((dy - 4) * 8);
+      }
+    }
+    const float d0 = __uint_as_float(r[R_DEPTH]), d1 = __uint_as_float(r[R_DEPTH + 1]),
+                d2 = __uint_as_float(r[R_DEPTH + 2]);
+    finite = isfinite(d0) && isfinite(d1) && isfinite(d2);
+    const float mag = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
+    const float margin = mag * 2.0e-6f + 1.0e-30f; /* > the rounding of pixdepth (~4e-7 relative) */
+    dlo = fminf(d0, fminf(d1, d2)) - margin;
+    dhi = fmaxf(d0, fmaxf(d1, d2)) + margin;
+  }
+  covered_total += __popc(mlo) + __popc(mhi);
+
+  /* conservative depth rejection of whole triangles against the sub-tile's depth range */
+  float tmax = __int_as_float(0xff800000), tmin = __int_as_float(0x7f800000);
+#pragma unroll
+  for(int p = 0; p < 2; p++)
+    if(in[p])
+    {
+      tmax = fmaxf(tmax, dep[p]);
+      tmin = fminf(tmin, dep[p]);
+    }
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1)
+  {
+    tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+    tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
+  }
+  const bool has = (mlo | mhi) != 0;
+  const u32 op = S_DEPTH_OP(st);
+  const bool writes = has && (st & S_DEPTH_WRITE);
+  const bool tested = (st & S_DEPTH_TEST) != 0;
+  /* can any triangle of this batch raise (lower) a stored depth? */
+  const bool raises = writes && !(tested && op <= 3u);
+  const bool lowers = writes && !(tested && (op == 0u || op == 2u || op == 4u || op == 6u));
+  const bool any_raise = __any_sync(0xffffffffu, raises);
+  const bool any_lower = __any_sync(0xffffffffu, lowers);
+  bool skip = false;
+  if(has && tested)
+  {
+    if(op == 0u)
+      skip = true;
+    else if(finite && !any_raise && ((op == 1u && dlo >= tmax) || (op == 3u && dlo > tmax)))
+      skip = true;
+    else if(finite && !any_lower && ((op == 4u && dhi <= tmin) || (op == 6u && dhi < tmin)))
+      skip = true;
+    else if(finite && !any_raise && !any_lower && op == 2u && (dlo > tmax || dhi < tmin))
+      skip = true;
+  }
+  const u32 live = __ballot_sync(0xffffffffu, has && !skip);
+  __syncwarp();
+
+  /* per-pixel coverage words: bit t set when triangle t covers the pixel */
+  u32 cov[2];
+  cov[0] = vgx_transpose32(mlo, lane) & live;
+  cov[1] = vgx_transpose32(mhi, lane) & live;
+  if(!in[0])
+    cov[0] = 0;
+  if(!in[1])
+    cov[1] = 0;
+
+  /* early depth test in primitive order per pixel */
+  u32 pass[2] = {0u, 0u};
+#pragma unroll
+  for(int p = 0; p < 2; p++)
+  {
+    u32 m = cov[p];
+    const int dy = ldy + 4 * p;
+    while(m)
+    {
+      const u32 t = __ffs(m) - 1;
+      m &= m - 1;
+      const VgxPlane pt = pl[t];
+      const u32 stt = pt.e.w;
+      float nn[3];
+      const float z = vgx_plane_depth(pt, sh.raw[t], ldx, dy, nn);
+      bool ok = true;
+      if(stt & S_DEPTH_TEST)
+        ok = vgx_depth_pass(S_DEPTH_OP(stt), z, dep[p]);
+      if(ok)
+      {
+        pass[p] |= 1u << t;
+        if(stt & S_DEPTH_WRITE)
+          dep[p] = z;
+      }
+    }
+  }
+  const u32 mine = __popc(pass[0]) + __popc(pass[1]);
+  shaded_total += mine;
+
+  /* compact the passing fragments across the warp */
+  u32 incl = mine;
+#pragma unroll
+  for(int o = 1; o < 32; o <<= 1)
+  {
+    u32 v = __shfl_up_sync(0xffffffffu, incl, o);
+    if(lane >= o)
+      incl += v;
+  }
+  const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+  const u32 excl = incl - mine;
+  u32 *soff = sh.off[wib];
+  soff[lane] = excl;
+  sh.pass[wib][lane][0] = pass[0];
+  sh.pass[wib][lane][1] = pass[1];
+  __syncwarp();
+
+  for(u32 chunk = 0; chunk < total; chunk += 32)
+  {
+    const u32 f = chunk + lane;
+    if(f < total)
+    {
+      u32 olo = 0, ohi = 31;
+      while(olo < ohi)
+      {
+        u32 mid = (olo + ohi + 1) >> 1;
+        if(soff[mid] <= f)
+          olo = mid;
+        else
+          ohi = mid - 1;
+      }
+      const u32 k = f - soff[olo];
+      const u32 p0 = sh.pass[wib][olo][0];
+      const u32 c0 = __popc(p0);
+      const int sel = k < c0 ? 0 : 1;
+      u32 m = sel ? sh.pass[wib][olo][1] : p0;
+      u32 kk = sel ? k - c0 : k;
+      while(kk--)
+        m &= m - 1;
+      const u32 t = __ffs(m) - 1;
+      const int fdx = (int)(olo & 7), fdy = (int)(olo >> 3) + 4 * sel;
+      const VgxPlane pt = pl[t];
+      const u32 *raw = sh.raw[t];
+      float nb[4];
+      (void)vgx_plane_depth(pt, raw, fdx, fdy, nb);
+      /* perspective correction, rasterizer.cpp:580-588 */
+      nb[0] = nb[0] * __uint_as_float(raw[R_INVW]);
+      nb[1] = nb[1] * __uint_as_float(raw[R_INVW + 1]);
+      nb[2] = nb[2] * __uint_as_float(raw[R_INVW + 2]);
+      const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
+      nb[0] = nb[0] * invlen;
+      nb[1] = nb[1] * invlen;
+      nb[2] = nb[2] * invlen;
+      nb[3] = 0.0f;
+      const float *iv = (const float *)(raw + VGX_REC_HEAD);
+      sh.col[wib][lane] = vgx_fs(draws[pt.b.w], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
+                                 __uint_as_float(raw[R_LOD]));
+    }
+    __syncwarp();
+    /* in-order blend: each owner consumes its fragments of this chunk */
+    const u32 lo_f = max(excl, chunk), hi_f = min(excl + mine, chunk + 32);
+    for(u32 g = lo_f; g < hi_f; g++)
+    {
+      const u32 k = g - excl;
+      const u32 c0 = __popc(pass[0]);
+      const int sel = k < c0 ? 0 : 1;
+      u32 m = sel ? pass[1] : pass[0];
+      u32 kk = sel ? k - c0 : k;
+      while(kk--)
+        m &= m - 1;
+      const u32 t = __ffs(m) - 1;
+      const float4 c = sh.col[wib][g - chunk];
+      const u32 stt = pl[t].e.w;
+      if(sel == 0)
+        col[0] = vgx_blend_write(stt, c, col[0]);
+      else
+        col[1] = vgx_blend_write(stt, c, col[1]);
+    }
+    __syncwarp();
+  }
+}
+
+/*
+ * Persistent raster: each CTA takes a bin tile from the queue; warp w owns the
+ * bin's 8x8 sub-tiles w, w + W, ...  The bin's triangle list (primitive order)
+ * is consumed in batches of 32 records staged once in shared memory for all
+ * warps.  Colour and depth of every owned pixel stay in registers until the
+ * bin is finished, then each pixel is written once.
+ */
+extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(VgxJob job)
+{
+  __shared__ VgxRasterShared sh;
   vgx_init_unorm8();
   __syncthreads();
 
@@ -370,21 +622,20 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32, 32 / VGX_RAS
   if(status[0] & VGX_STATUS_PAIR_OVERFLOW)
     return;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const VgxDraw *draws = (const VgxDraw *)job.draws;
   const VgxTarget *targets = (const VgxTarget *)job.targets;
   const u32 *vals = (const u32 *)job.vals;
   const u32 *tstart = (const u32 *)job.tile_start, *tend = (const u32 *)job.tile_end;
   const u32 nwork = job.all_tiles ? job.num_tiles : status[3];
-  u32(*tri)[VGX_REC] = s_tri[wib];
   u64 covered_total = 0, shaded_total = 0;
   const int ldx = lane & 7, ldy = lane >> 3;
 
   for(;;)
   {
-    u32 w = 0;
-    if(lane == 0)
-      w = atomicAdd(&status[2], 1u);
-    w = __shfl_sync(0xffffffffu, w, 0);
+    if(threadIdx.x == 0)
+      sh.bin = atomicAdd(&status[2], 1u);
+    __syncthreads();
+    const u32 w = sh.bin;
+    __syncthreads();
     if(w >= nwork)
       break;
     const u32 tile = job.work ? ((const u32 *)job.work)[w] : w;
@@ -400,30 +651,39 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32, 32 / VGX_RAS
     }
     const VgxTarget T = targets[lo];
     const u32 local = tile - T.tile_base;
-    const int x0 = (int)(local % T.tiles_x) << 3, y0 = (int)(local / T.tiles_x) << 3;
-    const int px = x0 + ldx;
-    int py[2];
-    py[0] = y0 + ldy;
-    py[1] = py[0] + 4;
-    bool in[2];
-    u32 col[2];
-    float dep[2];
+    const int bx0 = (int)(local % T.tiles_x) << VGX_TILE_SHIFT;
+    const int by0 = (int)(local / T.tiles_x) << VGX_TILE_SHIFT;
     u32 *cbuf = (u32 *)T.color;
     float *dbuf = (float *)T.depth;
+
+    int sx[VGX_SUBS_PER_WARP], sy[VGX_SUBS_PER_WARP];
+    bool valid[VGX_SUBS_PER_WARP];
+    bool in[VGX_SUBS_PER_WARP][2];
+    u32 col[VGX_SUBS_PER_WARP][2];
+    float dep[VGX_SUBS_PER_WARP][2];
 #pragma unroll
-    for(int p = 0; p < 2; p++)
+    for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
     {
-      in[p] = px < T.width && py[p] < T.height;
-      u64 pix = (u64)py[p] * (u32)T.width + (u32)px;
-      if(T.init_clear)
+      const int sub = wib + j * VGX_RASTER_WARPS;
+      valid[j] = sub < VGX_SUBS;
+      sx[j] = bx0 + (sub % VGX_SUB_EDGE) * 8;
+      sy[j] = by0 + (sub / VGX_SUB_EDGE) * 8;
+#pragma unroll
+      for(int p = 0; p < 2; p++)
       {
-        col[p] = T.clear_bgra;
-        dep[p] = T.clear_depth;
-      }
-      else
-      {
-        col[p] = in[p] ? cbuf[pix] : 0u;
-        dep[p] = (in[p] && dbuf) ? dbuf[pix] : 1.0f;
+        const int x = sx[j] + ldx, y = sy[j] + ldy + 4 * p;
+        in[j][p] = valid[j] && x < T.width && y < T.height;
+        const u64 pix = (u64)y * (u32)T.width + (u32)x;
+        if(T.init_clear)
+        {
+          col[j][p] = T.clear_bgra;
+          dep[j][p] = T.clear_depth;
+        }
+        else
+        {
+          col[j][p] = in[j][p] ? cbuf[pix] : 0u;
+          dep[j][p] = (in[j][p] && dbuf) ? dbuf[pix] : 1.0f;
+        }
       }
     }
 
@@ -431,253 +691,33 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32, 32 / VGX_RAS
     for(u32 base = start; base < end; base += 32)
     {
       const u32 n = min(32u, end - base);
-      /* lane t: its triangle's planes, coverage mask over the 8x8 tile, depth bounds */
-      u32 mlo = 0, mhi = 0, st = 0;
-      float dlo = 0.0f, dhi = 0.0f;
-      bool finite = false;
-      if((u32)lane < n)
+      /* stage the batch's records for every warp of the CTA */
+      for(u32 i = threadIdx.x; i < n * (VGX_REC / 4); i += VGX_RASTER_WARPS * 32)
       {
-        const u32 t = vals[base + lane];
-        const u32 *g = (const u32 *)job.records + (u64)t * VGX_REC;
-        int r[VGX_REC_HEAD];
-#pragma unroll
-        for(int q = 0; q < VGX_REC_HEAD; q += 4)
-        {
-          uint4 v = __ldg((const uint4 *)(g + q));
-          r[q] = (int)v.x;
-          r[q + 1] = (int)v.y;
-          r[q + 2] = (int)v.z;
-          r[q + 3] = (int)v.w;
-        }
-        const int v0x = r[R_V0X], v0y = r[R_V0Y], ABx = r[R_ABX], ABy = r[R_ABY];
-        const int ACx = r[R_ACX], ACy = r[R_ACY], bm = r[R_BARYMUL];
-        /* barycentric (rasterizer.cpp:303-309) expanded into affine planes in (x, y);
-           every product and sum is exact modulo 2^32, so each pixel's value equals the
-           reference's direct evaluation */
-        const int c1 = ACx * v0y - ACy * v0x, c2 = v0x * ABy - v0y * ABx;
-        const int a1 = bm * ACy, b1 = -(bm * ACx), a2 = -(bm * ABy), b2 = bm * ABx;
-        const int a0 = -(a1 + a2), b0 = -(b1 + b2);
-        const int e1 = a1 * x0 + b1 * y0 + bm * c1;
-        const int e2 = a2 * x0 + b2 * y0 + bm * c2;
-        const int e0 = a0 * x0 + b0 * y0 + bm * (r[R_AREA2] - c1 - c2);
-        st = (u32)r[R_STATE];
-        u32 *s = tri[lane];
-        *(uint4 *)(s + P_E) = make_uint4((u32)e0, (u32)e1, (u32)e2, st);
-        *(uint4 *)(s + P_A) = make_uint4((u32)a0, (u32)a1, (u32)a2, (u32)r[R_INVAREA]);
-        *(uint4 *)(s + P_B) = make_uint4((u32)b0, (u32)b1, (u32)b2, (u32)r[R_DRAW]);
-        *(uint4 *)(s + P_D) = make_uint4((u32)r[R_DEPTH], (u32)r[R_DEPTH + 1], (u32)r[R_DEPTH + 2],
-                                         (u32)r[R_LOD]);
-        *(uint4 *)(s + P_INVW) = make_uint4((u32)r[R_INVW], (u32)r[R_INVW + 1], (u32)r[R_INVW + 2], 0u);
-#pragma unroll
-        for(int q = VGX_REC_HEAD; q < VGX_REC; q += 4)
-          *(uint4 *)(s + q) = __ldg((const uint4 *)(g + q));
-        /* coverage of the tile, clipped to the bbox [min, max) (rasterizer.cpp:538-549) */
-        const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
-        const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
-        const int cx0 = max(minx - x0, 0), cx1 = min(maxx - x0, 8);
-        const int ry0 = max(miny - y0, 0), ry1 = min(maxy - y0, 8);
-        if(cx0 < cx1 && ry0 < ry1)
-        {
-          const u32 colmask = (0xffu >> (8 - cx1)) & (0xffu << cx0);
-          for(int dy = ry0; dy < ry1; dy++)
-          {
-            int q0 = e0 + b0 * dy, q1 = e1 + b1 * dy, q2 = e2 + b2 * dy;
-            u32 row = 0;
-#pragma unroll
-            for(int dx = 0; dx < 8; dx++)
-            {
-              row |= ((u32)(~(q0 | q1 | q2)) >> 31) << dx;
-              q0 += a0;
-              q1 += a1;
-              q2 += a2;
-            }
-            row &= colmask;
-            if(dy < 4)
-              mlo |= row << (dy * 8);
-            else
-              mhi |= row << ((dy - 4) * 8);
-          }
-        }
-        const float d0 = __int_as_float(r[R_DEPTH]), d1 = __int_as_float(r[R_DEPTH + 1]),
-                    d2 = __int_as_float(r[R_DEPTH + 2]);
-        finite = isfinite(d0) && isfinite(d1) && isfinite(d2);
-        const float mag = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
-        const float margin = mag * 2.0e-6f + 1.0e-30f; /* > the rounding of pixdepth (~4e-7 relative) */
-        dlo = fminf(d0, fminf(d1, d2)) - margin;
-        dhi = fmaxf(d0, fmaxf(d1, d2)) + margin;
+        const u32 t = i / (VGX_REC / 4), q = i % (VGX_REC / 4);
+        const uint4 *g = (const uint4 *)((const u32 *)job.records + (u64)vals[base + t] * VGX_REC);
+        ((uint4 *)sh.raw[t])[q] = __ldg(g + q);
       }
-      covered_total += __popc(mlo) + __popc(mhi);
-
-      /* conservative depth rejection of whole triangles against the tile's depth range */
-      float tmax = __int_as_float(0xff800000), tmin = __int_as_float(0x7f800000);
+      __syncthreads();
 #pragma unroll
-      for(int p = 0; p < 2; p++)
-        if(in[p])
-        {
-          tmax = fmaxf(tmax, dep[p]);
-          tmin = fminf(tmin, dep[p]);
-        }
-#pragma unroll
-      for(int o = 16; o > 0; o >>= 1)
-      {
-        tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
-        tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
-      }
-      const bool has = (mlo | mhi) != 0;
-      const u32 op = S_DEPTH_OP(st);
-      const bool writes = has && (st & S_DEPTH_WRITE);
-      const bool tested = (st & S_DEPTH_TEST) != 0;
-      /* can any triangle of this batch raise (lower) a stored depth? */
-      const bool raises = writes && !(tested && op <= 3u);
-      const bool lowers = writes && !(tested && (op == 0u || op == 2u || op == 4u || op == 6u));
-      const bool any_raise = __any_sync(0xffffffffu, raises);
-      const bool any_lower = __any_sync(0xffffffffu, lowers);
-      bool skip = false;
-      if(has && tested)
-      {
-        if(op == 0u)
-          skip = true;
-        else if(finite && !any_raise && ((op == 1u && dlo >= tmax) || (op == 3u && dlo > tmax)))
-          skip = true;
-        else if(finite && !any_lower && ((op == 4u && dhi <= tmin) || (op == 6u && dhi < tmin)))
-          skip = true;
-        else if(finite && !any_raise && !any_lower && op == 2u && (dlo > tmax || dhi < tmin))
-          skip = true;
-      }
-      const u32 live = __ballot_sync(0xffffffffu, has && !skip);
-      __syncwarp();
-
-      /* per-pixel coverage words: bit t set when triangle t covers the pixel */
-      u32 cov[2];
-      cov[0] = vgx_transpose32(mlo, lane) & live;
-      cov[1] = vgx_transpose32(mhi, lane) & live;
-      if(!in[0])
-        cov[0] = 0;
-      if(!in[1])
-        cov[1] = 0;
-
-      /* early depth test in primitive order per pixel */
-      u32 pass[2] = {0u, 0u};
-#pragma unroll
-      for(int p = 0; p < 2; p++)
-      {
-        u32 m = cov[p];
-        const int dy = ldy + 4 * p;
-        while(m)
-        {
-          const u32 t = __ffs(m) - 1;
-          m &= m - 1;
-          const u32 *s = tri[t];
-          const u32 stt = s[P_STATE];
-          float nn[3];
-          const float z = vgx_plane_depth(s, vgx_edge(s, 0, ldx, dy), vgx_edge(s, 1, ldx, dy),
-                                          vgx_edge(s, 2, ldx, dy), nn);
-          bool ok = true;
-          if(stt & S_DEPTH_TEST)
-            ok = vgx_depth_pass(S_DEPTH_OP(stt), z, dep[p]);
-          if(ok)
-          {
-            pass[p] |= 1u << t;
-            if(stt & S_DEPTH_WRITE)
-              dep[p] = z;
-          }
-        }
-      }
-      const u32 mine = __popc(pass[0]) + __popc(pass[1]);
-      shaded_total += mine;
-
-      /* compact the passing fragments across the warp */
-      u32 incl = mine;
-#pragma unroll
-      for(int o = 1; o < 32; o <<= 1)
-      {
-        u32 v = __shfl_up_sync(0xffffffffu, incl, o);
-        if(lane >= o)
-          incl += v;
-      }
-      const u32 total = __shfl_sync(0xffffffffu, incl, 31);
-      const u32 excl = incl - mine;
-      s_off[wib][lane] = excl;
-      s_pass[wib][lane][0] = pass[0];
-      s_pass[wib][lane][1] = pass[1];
-      __syncwarp();
-
-      for(u32 chunk = 0; chunk < total; chunk += 32)
-      {
-        const u32 f = chunk + lane;
-        if(f < total)
-        {
-          u32 olo = 0, ohi = 31;
-          while(olo < ohi)
-          {
-            u32 mid = (olo + ohi + 1) >> 1;
-            if(s_off[wib][mid] <= f)
-              olo = mid;
-            else
-              ohi = mid - 1;
-          }
-          const u32 k = f - s_off[wib][olo];
-          const u32 p0 = s_pass[wib][olo][0];
-          const u32 c0 = __popc(p0);
-          const int sel = k < c0 ? 0 : 1;
-          u32 m = sel ? s_pass[wib][olo][1] : p0;
-          u32 kk = sel ? k - c0 : k;
-          while(kk--)
-            m &= m - 1;
-          const u32 t = __ffs(m) - 1;
-          const int fdx = (int)(olo & 7), fdy = (int)(olo >> 3) + 4 * sel;
-          const u32 *s = tri[t];
-          float nb[4];
-          (void)vgx_plane_depth(s, vgx_edge(s, 0, fdx, fdy), vgx_edge(s, 1, fdx, fdy),
-                                vgx_edge(s, 2, fdx, fdy), nb);
-          /* perspective correction, rasterizer.cpp:580-588 */
-          nb[0] = nb[0] * __uint_as_float(s[P_INVW]);
-          nb[1] = nb[1] * __uint_as_float(s[P_INVW + 1]);
-          nb[2] = nb[2] * __uint_as_float(s[P_INVW + 2]);
-          const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
-          nb[0] = nb[0] * invlen;
-          nb[1] = nb[1] * invlen;
-          nb[2] = nb[2] * invlen;
-          nb[3] = 0.0f;
-          const float *iv = (const float *)(s + P_IV);
-          s_col[wib][lane] = vgx_fs(draws[s[P_DRAW]], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
-                                    __uint_as_float(s[P_LOD]));
-        }
-        __syncwarp();
-        /* in-order blend: each owner consumes its fragments of this chunk */
-        const u32 lo_f = max(excl, chunk), hi_f = min(excl + mine, chunk + 32);
-        for(u32 g = lo_f; g < hi_f; g++)
-        {
-          const u32 k = g - excl;
-          const u32 c0 = __popc(pass[0]);
-          const int sel = k < c0 ? 0 : 1;
-          u32 m = sel ? pass[1] : pass[0];
-          u32 kk = sel ? k - c0 : k;
-          while(kk--)
-            m &= m - 1;
-          const u32 t = __ffs(m) - 1;
-          const float4 c = s_col[wib][g - chunk];
-          const u32 stt = tri[t][P_STATE];
-          if(sel == 0)
-            col[0] = vgx_blend_write(stt, c, col[0]);
-          else
-            col[1] = vgx_blend_write(stt, c, col[1]);
-        }
-        __syncwarp();
-      }
+      for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
+        if(valid[j])
+          vgx_subtile_batch(job, sh, wib, lane, n, sx[j], sy[j], in[j], col[j], dep[j],
+                            covered_total, shaded_total);
+      __syncthreads();
     }
 
 #pragma unroll
-    for(int p = 0; p < 2; p++)
-    {
-      if(in[p])
-      {
-        u64 pix = (u64)py[p] * (u32)T.width + (u32)px;
-        cbuf[pix] = col[p];
-        if(dbuf)
-          dbuf[pix] = dep[p];
-      }
-    }
+    for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
+#pragma unroll
+      for(int p = 0; p < 2; p++)
+        if(in[j][p])
+        {
+          const u64 pix = (u64)(sy[j] + ldy + 4 * p) * (u32)T.width + (u32)(sx[j] + ldx);
+          cbuf[pix] = col[j][p];
+          if(dbuf)
+            dbuf[pix] = dep[j][p];
+        }
   }
   u64 *cnt = (u64 *)job.counters;
   vgx_warp_add_u64(&cnt[2], covered_total);

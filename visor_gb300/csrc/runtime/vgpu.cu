@@ -114,7 +114,7 @@ std::mutex g_mu;
 bool g_init = false;
 int g_sms = 148;
 int g_device = 0;
-vgpu_tuning g_tuning = {4, 1, 0};
+vgpu_tuning g_tuning = {0, 1, 0, 3, 1};
 
 /* ------------------------------------------------------------------------ */
 /* generic kernels                                                           */
@@ -464,11 +464,20 @@ extern "C" void vgpu_mem_free(void *dptr, void *hptr)
 /* programs (NVRTC)                                                          */
 /* ------------------------------------------------------------------------ */
 
-struct vgpu_program
+/* One compiled (bin tile, warps per bin) variant of a pipeline's stage kernels. */
+struct VgpuVariant
 {
   CUmodule mod = nullptr;
   CUfunction setup = nullptr, raster = nullptr;
-  u32 k = 0, rec_words = 0, tile_shift = 3;
+  u32 tile_shift = 3, warps = 1;
+};
+
+struct vgpu_program
+{
+  std::string source; /* translated shaders */
+  u32 k = 0, rec_words = 0;
+  std::map<u32, VgpuVariant *> variants; /* key: tile_shift << 8 | warps */
+  std::mutex mu;
 };
 
 static int compile_cubin(const std::string &src, std::vector<char> &cubin, char *log, size_t log_size)
@@ -510,10 +519,11 @@ static int compile_cubin(const std::string &src, std::vector<char> &cubin, char 
   return VGPU_OK;
 }
 
-static std::string full_source(const char *shader_source, uint32_t tile_shift)
+static std::string full_source(const char *shader_source, uint32_t tile_shift, uint32_t warps = 1)
 {
   std::string src;
   src += "#define VGX_TILE_SHIFT " + std::to_string(tile_shift) + "\n";
+  src += "#define VGX_RASTER_WARPS " + std::to_string(warps) + "\n";
   src += kVgxTypes;
   src += kVgxDevice;
   src += kVgxTiles;
@@ -526,10 +536,95 @@ extern "C" int vgpu_program_check(const char *shader_source, uint32_t tile_shift
                                   size_t log_size, uint64_t *cubin_bytes)
 {
   std::vector<char> cubin;
-  int rc = compile_cubin(full_source(shader_source, tile_shift), cubin, log, log_size);
+  /* tile_shift carries the warps per bin in bits 8..15 */
+  int rc = compile_cubin(full_source(shader_source, tile_shift & 0xff, std::max(1u, (tile_shift >> 8) & 0xff)),
+                         cubin, log, log_size);
   if(cubin_bytes)
     *cubin_bytes = cubin.size();
   return rc;
+}
+
+static int load_cubin(const std::string &src, std::vector<char> &cubin, char *log, size_t log_size)
+{
+  /* compiled images are cached in memory and on disk, keyed by the full source */
+  static std::map<u64, std::vector<char>> mem_cache;
+  const u64 h = hash_str(src + "|sm_103a|fmad=false");
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = mem_cache.find(h);
+    if(it != mem_cache.end())
+    {
+      cubin = it->second;
+      return VGPU_OK;
+    }
+  }
+  char path[1024];
+  snprintf(path, sizeof(path), "%s/%016llx.cubin", cache_dir().c_str(), (unsigned long long)h);
+  FILE *f = fopen(path, "rb");
+  if(f)
+  {
+    fseek(f, 0, SEEK_END);
+    long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    cubin.resize(n > 0 ? n : 0);
+    if(n <= 0 || fread(cubin.data(), 1, n, f) != (size_t)n)
+      cubin.clear();
+    fclose(f);
+  }
+  if(cubin.empty())
+  {
+    int rc = compile_cubin(src, cubin, log, log_size);
+    if(rc)
+      return rc;
+    std::string dir = cache_dir();
+    mkdir(dir.c_str(), 0755);
+    std::string tmp = std::string(path) + ".tmp" + std::to_string((long)getpid());
+    FILE *o = fopen(tmp.c_str(), "wb");
+    if(o)
+    {
+      fwrite(cubin.data(), 1, cubin.size(), o);
+      fclose(o);
+      rename(tmp.c_str(), path);
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  mem_cache[h] = cubin;
+  return VGPU_OK;
+}
+
+/* The variant of a program for a bin tile edge of 2^tile_shift pixels and
+   `warps` warps per bin; compiled with NVRTC on first use. */
+static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, int *rc_out)
+{
+  tile_shift = std::min<u32>(std::max<u32>(tile_shift, 3), 6);
+  const u32 subs = 1u << (2 * (tile_shift - 3));
+  warps = std::max<u32>(1, std::min<u32>(warps, std::min<u32>(subs, 16)));
+  const u32 key = tile_shift << 8 | warps;
+  std::lock_guard<std::mutex> lk(p->mu);
+  auto it = p->variants.find(key);
+  if(it != p->variants.end())
+    return it->second;
+  std::vector<char> cubin;
+  char log[4096] = {0};
+  int rc = load_cubin(full_source(p->source.c_str(), tile_shift, warps), cubin, log, sizeof(log));
+  if(rc)
+  {
+    *rc_out = rc;
+    return nullptr;
+  }
+  VgpuVariant *v = new VgpuVariant();
+  v->tile_shift = tile_shift;
+  v->warps = warps;
+  if(cudaSetDevice(g_device) != cudaSuccess || g_cu.moduleLoadData(&v->mod, cubin.data()) != CUDA_SUCCESS ||
+     g_cu.moduleGetFunction(&v->setup, v->mod, "vgx_setup") != CUDA_SUCCESS ||
+     g_cu.moduleGetFunction(&v->raster, v->mod, "vgx_raster") != CUDA_SUCCESS)
+  {
+    delete v;
+    *rc_out = VGPU_ERROR_DEVICE_LOST;
+    return nullptr;
+  }
+  p->variants[key] = v;
+  return v;
 }
 
 extern "C" int vgpu_program_create(const char *shader_source, uint32_t tile_shift,
@@ -541,63 +636,18 @@ extern "C" int vgpu_program_create(const char *shader_source, uint32_t tile_shif
   const char *kd = strstr(shader_source, "#define VGX_K ");
   if(!kd)
     return VGPU_ERROR_INITIALIZATION_FAILED;
-  u32 k = (u32)atoi(kd + 14);
-  std::string src = full_source(shader_source, tile_shift);
-
-  /* compiled images are cached in memory and on disk, keyed by the full source */
-  static std::map<u64, std::vector<char>> mem_cache;
-  const u64 h = hash_str(src + "|sm_103a|fmad=false");
-  std::vector<char> cubin;
-  CK(cudaSetDevice(g_device));
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    auto it = mem_cache.find(h);
-    if(it != mem_cache.end())
-      cubin = it->second;
-  }
-  char path[1024];
-  snprintf(path, sizeof(path), "%s/%016llx.cubin", cache_dir().c_str(), (unsigned long long)h);
-  if(cubin.empty())
-  {
-    FILE *f = fopen(path, "rb");
-    if(f)
-    {
-      fseek(f, 0, SEEK_END);
-      long n = ftell(f);
-      fseek(f, 0, SEEK_SET);
-      cubin.resize(n > 0 ? n : 0);
-      if(n <= 0 || fread(cubin.data(), 1, n, f) != (size_t)n)
-        cubin.clear();
-      fclose(f);
-    }
-  }
-  if(cubin.empty())
-  {
-    rc = compile_cubin(src, cubin, log, log_size);
-    if(rc)
-      return rc;
-    std::string dir = cache_dir();
-    mkdir(dir.c_str(), 0755);
-    std::string tmp = std::string(path) + ".tmp" + std::to_string((long)getpid());
-    FILE *f = fopen(tmp.c_str(), "wb");
-    if(f)
-    {
-      fwrite(cubin.data(), 1, cubin.size(), f);
-      fclose(f);
-      rename(tmp.c_str(), path);
-    }
-  }
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    mem_cache[h] = cubin;
-  }
   vgpu_program *p = new vgpu_program();
-  p->k = k;
-  p->tile_shift = tile_shift;
-  p->rec_words = ((20 + 3 * k) + 3) & ~3u;
-  CU(g_cu.moduleLoadData(&p->mod, cubin.data()));
-  CU(g_cu.moduleGetFunction(&p->setup, p->mod, "vgx_setup"));
-  CU(g_cu.moduleGetFunction(&p->raster, p->mod, "vgx_raster"));
+  p->source = shader_source;
+  p->k = (u32)atoi(kd + 14);
+  p->rec_words = ((20 + 3 * p->k) + 3) & ~3u;
+  /* compile the default variant now, as vkCreateGraphicsPipelines compiles */
+  if(!get_variant(p, tile_shift, g_tuning.raster_warps, &rc))
+  {
+    if(log && log_size)
+      snprintf(log, log_size, "stage kernel compilation failed");
+    delete p;
+    return rc;
+  }
   *out = p;
   return VGPU_OK;
 }
@@ -606,8 +656,12 @@ extern "C" void vgpu_program_destroy(vgpu_program *p)
 {
   if(!p)
     return;
-  if(p->mod)
-    g_cu.moduleUnload(p->mod);
+  for(auto &kv : p->variants)
+  {
+    if(kv.second->mod)
+      g_cu.moduleUnload(kv.second->mod);
+    delete kv.second;
+  }
   delete p;
 }
 
@@ -636,6 +690,7 @@ struct Cmd
 struct Job
 {
   vgpu_program *prog = nullptr;
+  VgpuVariant *var = nullptr;
   std::vector<VgxDraw> draws;
   std::vector<VgxTarget> targets;
   std::vector<u64> target_keys; /* colour address identifies a target */
@@ -830,9 +885,14 @@ static int list_build(vgpu_list *l)
     l->tris_in += ntris;
     if(!open || !batched || open->prog != c.prog)
     {
+      int vrc = VGPU_OK;
+      VgpuVariant *var = get_variant(c.prog, g_tuning.bin_shift, g_tuning.raster_warps, &vrc);
+      if(!var)
+        return vrc;
       l->jobs.emplace_back();
       open = &l->jobs.back();
       open->prog = c.prog;
+      open->var = var;
       Exec e;
       e.kind = Exec::E_JOB;
       e.index = l->jobs.size() - 1;
@@ -863,8 +923,8 @@ static int list_build(vgpu_list *l)
         }
         pending_clear.erase(pc);
       }
-      t.tiles_x = (u32)(t.width + (1 << open->prog->tile_shift) - 1) >> open->prog->tile_shift;
-      t.tiles_y = (u32)(t.height + (1 << open->prog->tile_shift) - 1) >> open->prog->tile_shift;
+      t.tiles_x = (u32)(t.width + (1 << open->var->tile_shift) - 1) >> open->var->tile_shift;
+      t.tiles_y = (u32)(t.height + (1 << open->var->tile_shift) - 1) >> open->var->tile_shift;
       t.tile_base = open->num_tiles;
       open->num_tiles += t.tiles_x * t.tiles_y;
       if(t.init_clear)
@@ -1092,7 +1152,7 @@ static VgxJob make_job(vgpu_queue *q, vgpu_list *l, Job &j, size_t ji)
   J.num_targets = (u32)j.targets.size();
   J.num_tiles = j.num_tiles;
   J.pair_capacity = q->pair_capacity;
-  J.tile_shift = j.prog->tile_shift;
+  J.tile_shift = j.var->tile_shift;
   J.key_bits = j.key_bits;
   J.all_tiles = j.all_tiles;
   (void)ji;
@@ -1117,7 +1177,7 @@ static int run_setup(vgpu_queue *q, vgpu_list *l, size_t ji)
     return VGPU_OK;
   }
   VgxJob J = make_job(q, l, j, ji);
-  int rc = launch(q, j.prog->setup, (j.num_tris + 255) / 256, 256, &J);
+  int rc = launch(q, j.var->setup, (j.num_tris + 255) / 256, 256, &J);
   if(rc)
     return rc;
   u32 *counts = l->d_counts + j.cnt_off;
@@ -1189,11 +1249,13 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
   }
   if(!j.all_tiles && !total)
     return VGPU_OK;
-  unsigned grid = std::max(1u, (unsigned)g_sms * g_tuning.raster_blocks_per_sm);
-  u32 warps_needed = j.all_tiles ? j.num_tiles : total;
-  const unsigned warps = j.prog->rec_words > 40 ? 4 : 8; /* VGX_RASTER_WARPS */
-  grid = std::min<unsigned>(grid, (warps_needed + warps - 1) / warps);
-  grid = std::max(grid, 1u);
+  /* persistent CTAs: enough to fill the SMs (32 warps each), never more than bins */
+  const unsigned warps = j.var->warps;
+  const unsigned per_sm = g_tuning.raster_blocks_per_sm ? g_tuning.raster_blocks_per_sm
+                                                        : std::max(1u, 32u / warps);
+  unsigned grid = std::max(1u, (unsigned)g_sms * per_sm);
+  const u32 bins = j.all_tiles ? j.num_tiles : total;
+  grid = std::max(1u, std::min<unsigned>(grid, bins));
   if(g_tuning.time_raster)
   {
     while(q->rev.size() < q->rev_used + 2)
@@ -1204,7 +1266,7 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
     }
     CK(cudaEventRecord(q->rev[q->rev_used], q->stream));
   }
-  int rc2 = launch(q, j.prog->raster, grid, warps * 32, &J);
+  int rc2 = launch(q, j.var->raster, grid, warps * 32, &J);
   if(g_tuning.time_raster)
   {
     CK(cudaEventRecord(q->rev[q->rev_used + 1], q->stream));

@@ -1,0 +1,34 @@
+"""Autotuner for the raster's bin tile and warps per bin.
+
+Every candidate renders the same pixels (the configuration only changes how
+work is binned and distributed), so the tuner may time candidates on the real
+command buffer.  Each candidate lowers the command buffer again, replays it a
+few times and keeps the fastest device time (CUDA events around the submit).
+"""
+import visor_gb300 as vg
+
+# (log2 bin edge, warps per bin): 8x8 ... 64x64 bins, 1 ... 16 warps
+CANDIDATES = [(3, 1), (4, 1), (4, 4), (5, 4), (5, 8), (5, 16), (6, 8), (6, 16)]
+
+
+def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
+    """Return (best (bin_shift, warps), {candidate: ms}) for a scene on a device."""
+    results = {}
+    vg.set_mode(mode)
+    for shift, warps in candidates or CANDIDATES:
+        vg.set_tuning(bin_shift=shift, raster_warps=warps)
+        up = dev.upload(handle, flags)
+        try:
+            up.submit()
+            best = None
+            for _ in range(reps):
+                dev.reset_stats()
+                up.submit()
+                ms = dev.stats()["gpu_ms"]
+                best = ms if best is None else min(best, ms)
+            results[(shift, warps)] = best
+        finally:
+            up.release()
+    choice = min(results, key=results.get)
+    vg.set_tuning(bin_shift=choice[0], raster_warps=choice[1])
+    return choice, results
