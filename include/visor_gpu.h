@@ -107,6 +107,7 @@ typedef struct vgpu_stats {
   double gpu_ms;       /* device time of the last submit (CUDA events on the queue's stream) */
   double raster_ms;    /* device time spent in raster kernels of the last submit */
   uint32_t status;     /* sticky device status bits */
+  uint64_t depth_tested; /* covered fragments that reached the per-pixel depth test (not rejected per triangle) */
 } vgpu_stats;
 int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out);
 void vgpu_queue_reset_stats(vgpu_queue *q);

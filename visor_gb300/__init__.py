@@ -32,7 +32,8 @@ class VgpuStats(C.Structure):
     _fields_ = [("tris_in", C.c_uint64), ("tris_out", C.c_uint64), ("tested", C.c_uint64),
                 ("covered", C.c_uint64), ("shaded", C.c_uint64), ("draws", C.c_uint64),
                 ("jobs", C.c_uint64), ("pairs", C.c_uint64), ("kernel_launches", C.c_uint64),
-                ("gpu_ms", C.c_double), ("raster_ms", C.c_double), ("status", C.c_uint32)]
+                ("gpu_ms", C.c_double), ("raster_ms", C.c_double), ("status", C.c_uint32),
+                ("depth_tested", C.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

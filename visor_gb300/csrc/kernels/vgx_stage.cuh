@@ -336,11 +336,14 @@ __device__ __forceinline__ u32 vgx_transpose32(u32 x, int lane)
 }
 
 /* per-warp plane of a batch triangle at the warp's sub-tile origin:
-   [0] e0 e1 e2 state, [1] x increments + invarea bits, [2] y increments + draw */
+   e = edge values at the origin + state, a = x steps + invarea bits,
+   b = y steps + record index, d = vertex depths + flags */
 struct VgxPlane
 {
-  uint4 e, a, b;
+  uint4 e, a, b, d;
 };
+
+#define PF_SMALL 1u /* area2 < 2^22: every covered pixel's barycentrics fit the exact fast int->float */
 
 __device__ __forceinline__ int vgx_edge(const VgxPlane &p, int k, int dx, int dy)
 {
@@ -350,40 +353,56 @@ __device__ __forceinline__ int vgx_edge(const VgxPlane &p, int k, int dx, int dy
   return (int)e + (int)a * dx + (int)b * dy;
 }
 
-__device__ __forceinline__ float vgx_plane_depth(const VgxPlane &p, const u32 *raw, int dx, int dy,
-                                                 float *n)
+/* float(v) for |v| < 2^22 without the quarter-rate conversion unit: 1.5*2^23 + v
+   is exact in binary32 (unit spacing), and subtracting 1.5*2^23 is exact. */
+__device__ __forceinline__ float vgx_i2f_small(int v)
 {
-  const float invarea = __uint_as_float(p.a.w);
-  n[0] = (float)vgx_edge(p, 0, dx, dy) * invarea;
-  n[1] = (float)vgx_edge(p, 1, dx, dy) * invarea;
-  n[2] = (float)vgx_edge(p, 2, dx, dy) * invarea;
-  return n[0] * __uint_as_float(raw[R_DEPTH]) + n[1] * __uint_as_float(raw[R_DEPTH + 1]) +
-         n[2] * __uint_as_float(raw[R_DEPTH + 2]);
+  return __int_as_float(0x4b400000 + v) - 12582912.0f;
 }
 
-struct VgxRasterShared
+__device__ __forceinline__ float vgx_plane_depth(const VgxPlane &p, int dx, int dy, float *n)
 {
-  u32 raw[32][VGX_REC] __attribute__((aligned(16))); /* the batch's records, shared by the CTA */
-  VgxPlane plane[VGX_RASTER_WARPS][32];
-  float4 col[VGX_RASTER_WARPS][32];
-  u32 pass[VGX_RASTER_WARPS][32][2];
-  u32 off[VGX_RASTER_WARPS][32];
-  u32 bin;
+  const float invarea = __uint_as_float(p.a.w);
+  const int b0 = vgx_edge(p, 0, dx, dy), b1 = vgx_edge(p, 1, dx, dy), b2 = vgx_edge(p, 2, dx, dy);
+  if(p.d.w & PF_SMALL)
+  {
+    n[0] = vgx_i2f_small(b0) * invarea;
+    n[1] = vgx_i2f_small(b1) * invarea;
+    n[2] = vgx_i2f_small(b2) * invarea;
+  }
+  else
+  {
+    n[0] = (float)b0 * invarea;
+    n[1] = (float)b1 * invarea;
+    n[2] = (float)b2 * invarea;
+  }
+  return n[0] * __uint_as_float(p.d.x) + n[1] * __uint_as_float(p.d.y) +
+         n[2] * __uint_as_float(p.d.z);
+}
+
+struct VgxWarpShared
+{
+  VgxPlane plane[32];
+  float4 col[32];
+  u32 pass[32][2];
+  u32 off[32];
 };
 
 /*
- * One warp, one 8x8 sub-tile at (x0, y0), one batch of n <= 32 triangles
- * already in shared memory.  Lane L owns pixels (L&7, L>>3) and (L&7, (L>>3)+4);
- * their colour and depth live in col[]/dep[] for the whole bin.
+ * One warp, one 8x8 sub-tile at (x0, y0), one batch of n <= 32 triangles whose
+ * record headers lane t holds in r[] (triangle t).  Lane L owns pixels
+ * (L&7, L>>3) and (L&7, (L>>3)+4); their colour and depth live in col[]/dep[]
+ * for the whole bin.
  */
-__device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterShared &sh, int wib,
-                                                  int lane, u32 n, int x0, int y0, const bool *in,
-                                                  u32 *col, float *dep, u64 &covered_total,
-                                                  u64 &shaded_total)
+__device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShared &sh, int lane,
+                                                  u32 n, const int *r, u32 rec_index, int x0, int y0,
+                                                  const bool *in, u32 *col, float *dep,
+                                                  u64 &covered_total, u64 &shaded_total,
+                                                  u64 &tested_total)
 {
   const VgxDraw *draws = (const VgxDraw *)job.draws;
   const int ldx = lane & 7, ldy = lane >> 3;
-  VgxPlane *pl = sh.plane[wib];
+  VgxPlane *pl = sh.plane;
 
   /* lane t: its triangle's planes at the sub-tile origin, coverage mask, depth bounds */
   u32 mlo = 0, mhi = 0, st = 0;
@@ -391,9 +410,8 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
   bool finite = false;
   if((u32)lane < n)
   {
-    const u32 *r = sh.raw[lane];
-    const int v0x = (int)r[R_V0X], v0y = (int)r[R_V0Y], ABx = (int)r[R_ABX], ABy = (int)r[R_ABY];
-    const int ACx = (int)r[R_ACX], ACy = (int)r[R_ACY], bm = (int)r[R_BARYMUL];
+    const int v0x = r[R_V0X], v0y = r[R_V0Y], ABx = r[R_ABX], ABy = r[R_ABY];
+    const int ACx = r[R_ACX], ACy = r[R_ACY], bm = r[R_BARYMUL];
     /* barycentric (rasterizer.cpp:303-309) expanded into affine planes in (x, y);
        every product and sum is exact modulo 2^32, so each pixel's value equals the
        reference's direct evaluation */
@@ -402,16 +420,19 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
     const int a0 = -(a1 + a2), b0 = -(b1 + b2);
     const int e1 = a1 * x0 + b1 * y0 + bm * c1;
     const int e2 = a2 * x0 + b2 * y0 + bm * c2;
-    const int e0 = a0 * x0 + b0 * y0 + bm * ((int)r[R_AREA2] - c1 - c2);
-    st = r[R_STATE];
+    const int e0 = a0 * x0 + b0 * y0 + bm * (r[R_AREA2] - c1 - c2);
+    st = (u32)r[R_STATE];
+    const int area = r[R_AREA2] < 0 ? -r[R_AREA2] : r[R_AREA2];
     VgxPlane p;
     p.e = make_uint4((u32)e0, (u32)e1, (u32)e2, st);
-    p.a = make_uint4((u32)a0, (u32)a1, (u32)a2, r[R_INVAREA]);
-    p.b = make_uint4((u32)b0, (u32)b1, (u32)b2, r[R_DRAW]);
+    p.a = make_uint4((u32)a0, (u32)a1, (u32)a2, (u32)r[R_INVAREA]);
+    p.b = make_uint4((u32)b0, (u32)b1, (u32)b2, rec_index);
+    p.d = make_uint4((u32)r[R_DEPTH], (u32)r[R_DEPTH + 1], (u32)r[R_DEPTH + 2],
+                     area < (1 << 22) ? PF_SMALL : 0u);
     pl[lane] = p;
     /* coverage of the sub-tile, clipped to the bbox [min, max) (rasterizer.cpp:538-549) */
-    const int minx = (int)(r[R_MIN] & 0xffffu), miny = (int)(r[R_MIN] >> 16);
-    const int maxx = (int)(r[R_MAX] & 0xffffu), maxy = (int)(r[R_MAX] >> 16);
+    const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
+    const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
     const int cx0 = max(minx - x0, 0), cx1 = min(maxx - x0, 8);
     const int ry0 = max(miny - y0, 0), ry1 = min(maxy - y0, 8);
     if(cx0 < cx1 && ry0 < ry1)
@@ -436,8 +457,8 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
           mhi |= row << ((dy - 4) * 8);
       }
     }
-    const float d0 = __uint_as_float(r[R_DEPTH]), d1 = __uint_as_float(r[R_DEPTH + 1]),
-                d2 = __uint_as_float(r[R_DEPTH + 2]);
+    const float d0 = __int_as_float(r[R_DEPTH]), d1 = __int_as_float(r[R_DEPTH + 1]),
+                d2 = __int_as_float(r[R_DEPTH + 2]);
     finite = isfinite(d0) && isfinite(d1) && isfinite(d2);
     const float mag = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
     const float margin = mag * 2.0e-6f + 1.0e-30f; /* > the rounding of pixdepth (~4e-7 relative) */
@@ -493,6 +514,7 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
     cov[0] = 0;
   if(!in[1])
     cov[1] = 0;
+  tested_total += __popc(cov[0]) + __popc(cov[1]);
 
   /* early depth test in primitive order per pixel */
   u32 pass[2] = {0u, 0u};
@@ -508,7 +530,7 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
       const VgxPlane pt = pl[t];
       const u32 stt = pt.e.w;
       float nn[3];
-      const float z = vgx_plane_depth(pt, sh.raw[t], ldx, dy, nn);
+      const float z = vgx_plane_depth(pt, ldx, dy, nn);
       bool ok = true;
       if(stt & S_DEPTH_TEST)
         ok = vgx_depth_pass(S_DEPTH_OP(stt), z, dep[p]);
@@ -534,10 +556,9 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
   }
   const u32 total = __shfl_sync(0xffffffffu, incl, 31);
   const u32 excl = incl - mine;
-  u32 *soff = sh.off[wib];
-  soff[lane] = excl;
-  sh.pass[wib][lane][0] = pass[0];
-  sh.pass[wib][lane][1] = pass[1];
+  sh.off[lane] = excl;
+  sh.pass[lane][0] = pass[0];
+  sh.pass[lane][1] = pass[1];
   __syncwarp();
 
   for(u32 chunk = 0; chunk < total; chunk += 32)
@@ -549,44 +570,47 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
       while(olo < ohi)
       {
         u32 mid = (olo + ohi + 1) >> 1;
-        if(soff[mid] <= f)
+        if(sh.off[mid] <= f)
           olo = mid;
         else
           ohi = mid - 1;
       }
-      const u32 k = f - soff[olo];
-      const u32 p0 = sh.pass[wib][olo][0];
+      const u32 k = f - sh.off[olo];
+      const u32 p0 = sh.pass[olo][0];
       const u32 c0 = __popc(p0);
       const int sel = k < c0 ? 0 : 1;
-      u32 m = sel ? sh.pass[wib][olo][1] : p0;
+      u32 m = sel ? sh.pass[olo][1] : p0;
       u32 kk = sel ? k - c0 : k;
       while(kk--)
         m &= m - 1;
       const u32 t = __ffs(m) - 1;
       const int fdx = (int)(olo & 7), fdy = (int)(olo >> 3) + 4 * sel;
       const VgxPlane pt = pl[t];
-      const u32 *raw = sh.raw[t];
+      const u32 *g = (const u32 *)job.records + (u64)pt.b.w * VGX_REC;
       float nb[4];
-      (void)vgx_plane_depth(pt, raw, fdx, fdy, nb);
+      (void)vgx_plane_depth(pt, fdx, fdy, nb);
       /* perspective correction, rasterizer.cpp:580-588 */
-      nb[0] = nb[0] * __uint_as_float(raw[R_INVW]);
-      nb[1] = nb[1] * __uint_as_float(raw[R_INVW + 1]);
-      nb[2] = nb[2] * __uint_as_float(raw[R_INVW + 2]);
+      nb[0] = nb[0] * __uint_as_float(__ldg(g + R_INVW));
+      nb[1] = nb[1] * __uint_as_float(__ldg(g + R_INVW + 1));
+      nb[2] = nb[2] * __uint_as_float(__ldg(g + R_INVW + 2));
       const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
       nb[0] = nb[0] * invlen;
       nb[1] = nb[1] * invlen;
       nb[2] = nb[2] * invlen;
       nb[3] = 0.0f;
-      const float *iv = (const float *)(raw + VGX_REC_HEAD);
-      sh.col[wib][lane] = vgx_fs(draws[pt.b.w], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
-                                 __uint_as_float(raw[R_LOD]));
+      float iv[3 * (VGX_K > 0 ? VGX_K : 1)];
+#pragma unroll
+      for(int q = 0; q < 3 * VGX_K; q++)
+        iv[q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + q));
+      sh.col[lane] = vgx_fs(draws[__ldg(g + R_DRAW)], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
+                            __uint_as_float(__ldg(g + R_LOD)));
     }
     __syncwarp();
     /* in-order blend: each owner consumes its fragments of this chunk */
     const u32 lo_f = max(excl, chunk), hi_f = min(excl + mine, chunk + 32);
-    for(u32 g = lo_f; g < hi_f; g++)
+    for(u32 gg = lo_f; gg < hi_f; gg++)
     {
-      const u32 k = g - excl;
+      const u32 k = gg - excl;
       const u32 c0 = __popc(pass[0]);
       const int sel = k < c0 ? 0 : 1;
       u32 m = sel ? pass[1] : pass[0];
@@ -594,7 +618,7 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
       while(kk--)
         m &= m - 1;
       const u32 t = __ffs(m) - 1;
-      const float4 c = sh.col[wib][g - chunk];
+      const float4 c = sh.col[gg - chunk];
       const u32 stt = pl[t].e.w;
       if(sel == 0)
         col[0] = vgx_blend_write(stt, c, col[0]);
@@ -607,14 +631,16 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxRasterSh
 
 /*
  * Persistent raster: each CTA takes a bin tile from the queue; warp w owns the
- * bin's 8x8 sub-tiles w, w + W, ...  The bin's triangle list (primitive order)
- * is consumed in batches of 32 records staged once in shared memory for all
- * warps.  Colour and depth of every owned pixel stay in registers until the
- * bin is finished, then each pixel is written once.
+ * bin's 8x8 sub-tiles w, w + W, ...  Every warp walks the bin's triangle list
+ * (primitive order) in batches of 32 on its own (lane t loads record t; the
+ * warps of a CTA share those loads through L1), so warps never wait for each
+ * other.  Colour and depth of every owned pixel stay in registers until the bin
+ * is finished, then each pixel is written once.
  */
 extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(VgxJob job)
 {
-  __shared__ VgxRasterShared sh;
+  __shared__ VgxWarpShared wsh[VGX_RASTER_WARPS];
+  __shared__ u32 s_bin;
   vgx_init_unorm8();
   __syncthreads();
 
@@ -626,15 +652,16 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
   const u32 *vals = (const u32 *)job.vals;
   const u32 *tstart = (const u32 *)job.tile_start, *tend = (const u32 *)job.tile_end;
   const u32 nwork = job.all_tiles ? job.num_tiles : status[3];
-  u64 covered_total = 0, shaded_total = 0;
+  u64 covered_total = 0, shaded_total = 0, tested_total = 0;
   const int ldx = lane & 7, ldy = lane >> 3;
+  VgxWarpShared &sh = wsh[wib];
 
   for(;;)
   {
     if(threadIdx.x == 0)
-      sh.bin = atomicAdd(&status[2], 1u);
+      s_bin = atomicAdd(&status[2], 1u);
     __syncthreads();
-    const u32 w = sh.bin;
+    const u32 w = s_bin;
     __syncthreads();
     if(w >= nwork)
       break;
@@ -687,24 +714,35 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
       }
     }
 
+    bool any_valid = false;
+#pragma unroll
+    for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
+      any_valid |= valid[j];
     const u32 start = tstart[tile], end = tend[tile];
-    for(u32 base = start; base < end; base += 32)
+    for(u32 base = start; any_valid && base < end; base += 32)
     {
       const u32 n = min(32u, end - base);
-      /* stage the batch's records for every warp of the CTA */
-      for(u32 i = threadIdx.x; i < n * (VGX_REC / 4); i += VGX_RASTER_WARPS * 32)
+      int r[VGX_REC_HEAD];
+      u32 rec_index = 0;
+      if((u32)lane < n)
       {
-        const u32 t = i / (VGX_REC / 4), q = i % (VGX_REC / 4);
-        const uint4 *g = (const uint4 *)((const u32 *)job.records + (u64)vals[base + t] * VGX_REC);
-        ((uint4 *)sh.raw[t])[q] = __ldg(g + q);
+        rec_index = vals[base + lane];
+        const u32 *g = (const u32 *)job.records + (u64)rec_index * VGX_REC;
+#pragma unroll
+        for(int q = 0; q < VGX_REC_HEAD; q += 4)
+        {
+          const uint4 v = __ldg((const uint4 *)(g + q));
+          r[q] = (int)v.x;
+          r[q + 1] = (int)v.y;
+          r[q + 2] = (int)v.z;
+          r[q + 3] = (int)v.w;
+        }
       }
-      __syncthreads();
 #pragma unroll
       for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
         if(valid[j])
-          vgx_subtile_batch(job, sh, wib, lane, n, sx[j], sy[j], in[j], col[j], dep[j],
-                            covered_total, shaded_total);
-      __syncthreads();
+          vgx_subtile_batch(job, sh, lane, n, r, rec_index, sx[j], sy[j], in[j], col[j], dep[j],
+                            covered_total, shaded_total, tested_total);
     }
 
 #pragma unroll
@@ -722,6 +760,7 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
   u64 *cnt = (u64 *)job.counters;
   vgx_warp_add_u64(&cnt[2], covered_total);
   vgx_warp_add_u64(&cnt[3], shaded_total);
+  vgx_warp_add_u64(&cnt[4], tested_total);
 }
 
 #endif

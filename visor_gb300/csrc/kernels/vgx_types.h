@@ -115,7 +115,7 @@ typedef struct VgxJob {
   u64 tile_start, tile_end;           /* u32* per tile */
   u64 work;                           /* u32* tiles to raster; 0 = every tile in order */
   u64 status;                         /* u32*: [0] flags, [1] pair total, [2] work queue, [3] work count */
-  u64 counters;                       /* u64*: tris_out, tested, covered, shaded */
+  u64 counters;                       /* u64*: tris_out, tested, covered, shaded, depth-tested */
   u64 scratch;                        /* u32* scan/sort scratch */
   u32 num_draws, num_tris;
   u32 num_targets, num_tiles;

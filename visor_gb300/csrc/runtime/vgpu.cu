@@ -995,7 +995,7 @@ struct vgpu_queue
   u32 *scratch = nullptr;
   u64 scratch_words = 0;
   u32 *status = nullptr;  /* 4 words per job slot */
-  u64 *counters = nullptr; /* tris_out, tested, covered, shaded */
+  u64 *counters = nullptr; /* tris_out, tested, covered, shaded, depth-tested after hierarchical Z */
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> rev; /* raster start/stop pairs of the last submit */
   size_t rev_used = 0;
@@ -1022,8 +1022,8 @@ extern "C" int vgpu_queue_create(vgpu_queue **out)
   CK(cudaStreamCreateWithFlags(&q->stream, cudaStreamNonBlocking));
   CK(cudaMalloc(&q->status, 64));
   CK(cudaMemset(q->status, 0, 64));
-  CK(cudaMalloc(&q->counters, 4 * sizeof(u64)));
-  CK(cudaMemset(q->counters, 0, 4 * sizeof(u64)));
+  CK(cudaMalloc(&q->counters, 8 * sizeof(u64)));
+  CK(cudaMemset(q->counters, 0, 8 * sizeof(u64)));
   CK(cudaEventCreate(&q->ev0));
   CK(cudaEventCreate(&q->ev1));
   memset(&q->stats, 0, sizeof(q->stats));
@@ -1431,7 +1431,7 @@ extern "C" int vgpu_queue_wait_idle(vgpu_queue *q)
 extern "C" int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out)
 {
   CK(cudaStreamSynchronize(q->stream));
-  u64 c[4];
+  u64 c[8];
   CK(cudaMemcpy(c, q->counters, sizeof(c), cudaMemcpyDeviceToHost));
   u32 st = 0;
   CK(cudaMemcpy(&st, q->status, 4, cudaMemcpyDeviceToHost));
@@ -1440,6 +1440,7 @@ extern "C" int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out)
   out->tested = c[1];
   out->covered = c[2];
   out->shaded = c[3];
+  out->depth_tested = c[4];
   out->status = st;
   out->kernel_launches = q->launches;
   float ms = 0.0f;
@@ -1455,7 +1456,7 @@ extern "C" int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out)
 extern "C" void vgpu_queue_reset_stats(vgpu_queue *q)
 {
   cudaStreamSynchronize(q->stream);
-  cudaMemset(q->counters, 0, 4 * sizeof(u64));
+  cudaMemset(q->counters, 0, 8 * sizeof(u64));
   cudaMemset(q->status, 0, 4);
   memset(&q->stats, 0, sizeof(q->stats));
   q->launches = 0;
