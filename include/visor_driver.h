@@ -62,6 +62,9 @@ void vsd_release(vsd_scene *s);
 /* The VkQueue the context submits to. */
 void *vsd_queue(vsd_context *ctx);
 
+/* The VkCommandBuffer the scene recorded (for callers that submit it themselves). */
+void *vsd_command_buffer(vsd_scene *s);
+
 /* Bytes copied host->device per submit when VSD_RESTAGE_INPUTS is set. */
 uint64_t vsd_restage_bytes(const vsd_scene *s);
 

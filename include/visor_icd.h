@@ -48,6 +48,35 @@ void visor_gb300_queue_reset_stats(VkQueue queue);
 /* Overwrite a buffer larger than L2 on the queue (benchmark hygiene between timed steps). */
 int visor_gb300_flush_l2(VkQueue queue);
 
+/*
+ * vkQueueSubmit that makes no device allocation.  No counterpart in the
+ * reference (its submit runs on the CPU and has no device memory to grow).
+ *
+ * vkQueueSubmit sizes the queue's binning buffers (tile pairs and their sort
+ * ping-pong, tile ranges, histograms) to each frame and grows them with
+ * cudaMalloc/cudaFree when a frame needs more than any before.  Some callers
+ * cannot take that: a frame loop with a latency bound, where cudaFree waits for
+ * all work on the device and stalls every other stream; a process whose device
+ * memory is committed up front (a serving loop that admits frames against a
+ * fixed budget, or one that shares the GPU with an allocator that owns the
+ * rest of HBM), where growth at run time can fail halfway through a frame.
+ * This call takes all of that storage from one fixed 18.5 MiB device array.
+ *
+ * - Every command buffer must have gone through vkQueueSubmit once (that
+ *   lowers it and allocates its own storage); otherwise
+ *   VK_ERROR_INITIALIZATION_FAILED.
+ * - A job over 1,048,576 tile pairs or 131,072 bin tiles is rejected with
+ *   VK_ERROR_OUT_OF_DEVICE_MEMORY and a message on stderr (the pair count is
+ *   known only after the job's setup, so segments of the submission before a
+ *   rejected one have run).
+ * - The first call on a device looks up the array's device address: make it
+ *   before any stream capture.
+ * - The array is one per device: calls on different queues that overlap in
+ *   time race on it.  Calls on one queue are ordered by its stream.
+ */
+VkResult visor_gb300_queue_submit_noalloc(VkQueue queue, uint32_t submitCount,
+                                          const VkSubmitInfo *pSubmits, VkFence fence);
+
 /* SPIR-V pair -> CUDA source, without a device (returns 0 and err on failure). */
 size_t visor_gb300_translate(const uint32_t *vs_words, size_t vs_count, const uint32_t *fs_words,
                              size_t fs_count, char *out, size_t size, char *err, size_t err_size);

@@ -1,0 +1,149 @@
+"""The allocation-free submit against vkQueueSubmit, through the C ABI.
+
+visor_gb300_queue_submit_noalloc replays command buffers that vkQueueSubmit
+has lowered, with the binning storage taken from a fixed device array.  Each
+scene is submitted once through vkQueueSubmit (the expected frame and
+counters), then twice in a row through the allocation-free call; both frames
+must equal the first bit for bit, and the rasterizer counters of each call must
+equal those of the ordinary submit (so the work was redone, not left over).
+The file sorts last so that it also runs after every other GPU test in one
+process; it passes alone in a fresh process too.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import visor_gb300 as vg
+from visor_gb300 import scene as vs
+import scenes_edge
+
+pytestmark = pytest.mark.gpu
+
+VK_SUCCESS = 0
+VK_ERROR_OUT_OF_DEVICE_MEMORY = -2
+VK_ERROR_INITIALIZATION_FAILED = -3
+VK_STRUCTURE_TYPE_SUBMIT_INFO = 4
+COUNTERS = ("tris_in", "tris_out", "tested", "covered", "shaded", "depth_tested", "pairs", "draws")
+
+
+class SubmitInfo(C.Structure):
+    _fields_ = [("sType", C.c_int), ("pNext", C.c_void_p),
+                ("waitSemaphoreCount", C.c_uint32), ("pWaitSemaphores", C.c_void_p),
+                ("pWaitDstStageMask", C.c_void_p),
+                ("commandBufferCount", C.c_uint32), ("pCommandBuffers", C.POINTER(C.c_void_p)),
+                ("signalSemaphoreCount", C.c_uint32), ("pSignalSemaphores", C.c_void_p)]
+
+
+def _bind(L):
+    L.visor_gb300_queue_submit_noalloc.argtypes = [C.c_void_p, C.c_uint32,
+                                                   C.POINTER(SubmitInfo), C.c_void_p]
+    L.visor_gb300_queue_submit_noalloc.restype = C.c_int
+    L.vsd_command_buffer.argtypes = [C.c_void_p]
+    L.vsd_command_buffer.restype = C.c_void_p
+    L.vkQueueWaitIdle.argtypes = [C.c_void_p]
+    L.vkQueueWaitIdle.restype = C.c_int
+    return L
+
+
+@pytest.fixture(scope="module")
+def device():
+    d = vg.Device()
+    _bind(d.lib)
+    yield d
+    d.close()
+
+
+@pytest.fixture
+def restore_mode_and_tuning():
+    mode, tuning = vg.lib().visor_gb300_get_mode(), vg.get_tuning()
+    yield
+    vg.set_mode(mode)
+    vg.set_tuning(**tuning)
+
+
+def submit_noalloc(dev, up):
+    cb = (C.c_void_p * 1)(dev.lib.vsd_command_buffer(up.sc))
+    info = SubmitInfo(sType=VK_STRUCTURE_TYPE_SUBMIT_INFO, commandBufferCount=1, pCommandBuffers=cb)
+    rc = dev.lib.visor_gb300_queue_submit_noalloc(dev.queue, 1, C.byref(info), None)
+    if rc == VK_SUCCESS:
+        assert dev.lib.vkQueueWaitIdle(dev.queue) == VK_SUCCESS
+    return rc
+
+
+def counters(dev):
+    s = dev.stats()
+    assert s["status"] == 0, s
+    return {k: s[k] for k in COUNTERS}
+
+
+SCENES = ["cfg2_medium_blend", "cfg1_frames4", "cfg3_small_bilinear", "cfg4_small"]
+
+
+@pytest.mark.parametrize("mode", ["batched", "per_draw"])
+@pytest.mark.parametrize("name", SCENES)
+def test_noalloc_matches_queue_submit(device, restore_mode_and_tuning, name, mode):
+    vg.set_mode(vg.MODE_BATCHED if mode == "batched" else vg.MODE_PER_DRAW)
+    h = scenes_edge.build(device.lib, name)
+    up = device.upload(h)
+    try:
+        device.reset_stats()
+        up.submit()
+        want_cols, want_deps = up.read()
+        want = counters(device)
+        assert want["shaded"] > 0
+        for call in range(2):
+            device.reset_stats()
+            assert submit_noalloc(device, up) == VK_SUCCESS
+            got = counters(device)
+            assert got == want, (call, got, want)
+            cols, deps = up.read()
+            for t, (c, d, wc, wd) in enumerate(zip(cols, deps, want_cols, want_deps)):
+                assert np.array_equal(c, wc), (call, t)
+                assert np.array_equal(d.view(np.uint32), wd.view(np.uint32)), (call, t)
+    finally:
+        up.release()
+
+
+def test_noalloc_needs_a_lowered_command_buffer(device):
+    h = scenes_edge.build(device.lib, "cfg1_sphere")
+    up = device.upload(h)
+    try:
+        assert submit_noalloc(device, up) == VK_ERROR_INITIALIZATION_FAILED
+        up.submit()
+        assert submit_noalloc(device, up) == VK_SUCCESS
+    finally:
+        up.release()
+
+
+def test_noalloc_rejects_too_many_tiles(device, restore_mode_and_tuning):
+    """A 4096x4096 target in 8x8 bins has 262,144 tiles; the fixed array holds 131,072."""
+    vg.set_mode(vg.MODE_BATCHED)
+    vg.set_tuning(bin_shift=3, raster_warps=1)
+    h = vs.generate(device.lib, vs.CFG_TRIS, 5, width=4096, height=4096, count=200, max_area=500.0)
+    up = device.upload(h)
+    try:
+        up.submit()
+        want_cols, _ = up.read()
+        assert submit_noalloc(device, up) == VK_ERROR_OUT_OF_DEVICE_MEMORY
+        up.submit()
+        cols, _ = up.read()
+        assert np.array_equal(cols[0], want_cols[0])
+    finally:
+        up.release()
+
+
+def test_noalloc_rejects_too_many_pairs(device, restore_mode_and_tuning):
+    """About three million (tile, triangle) pairs in 8x8 bins; the fixed array holds 1,048,576."""
+    vg.set_mode(vg.MODE_BATCHED)
+    vg.set_tuning(bin_shift=3, raster_warps=1)
+    h = vs.generate(device.lib, vs.CFG_TRIS, 6, width=1920, height=1080, count=20000,
+                    max_area=100000.0)
+    up = device.upload(h)
+    try:
+        device.reset_stats()
+        up.submit()
+        assert device.stats()["pairs"] > (1 << 20)
+        assert submit_noalloc(device, up) == VK_ERROR_OUT_OF_DEVICE_MEMORY
+    finally:
+        up.release()

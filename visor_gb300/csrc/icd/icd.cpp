@@ -32,6 +32,7 @@
 
 #include "visor_icd.h"
 #include "../spirv/translate.h"
+#include "../runtime/vgpu_noalloc.h"
 
 #define VISOR_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -1618,6 +1619,35 @@ VISOR_EXPORT VkResult vk_icdNegotiateLoaderICDInterfaceVersion(uint32_t *pSuppor
 /* ------------------------------------------------------------------------ */
 /* project extensions                                                        */
 /* ------------------------------------------------------------------------ */
+
+/* vkQueueSubmit without device allocation: command buffers that vkQueueSubmit
+   has already lowered are replayed with their binning storage taken from a
+   fixed device array (vgpu_submit_noalloc). */
+VISOR_EXPORT VkResult visor_gb300_queue_submit_noalloc(VkQueue q, uint32_t n,
+                                                       const VkSubmitInfo *submits, VkFence fence)
+{
+  for(uint32_t i = 0; i < n; i++)
+    for(uint32_t c = 0; c < submits[i].commandBufferCount; c++)
+    {
+      VkCommandBuffer cb = submits[i].pCommandBuffers[c];
+      if(!cb->lowered || !cb->list)
+      {
+        fprintf(stderr, "visor_gb300: visor_gb300_queue_submit_noalloc: command buffer has not been "
+                        "submitted through vkQueueSubmit yet\n");
+        return VK_ERROR_INITIALIZATION_FAILED;
+      }
+      int rc = vgpu_submit_noalloc(q->q, cb->list);
+      if(rc)
+        return vr(rc);
+    }
+  if(fence)
+  {
+    int rc = vgpu_fence_signal(q->q, fence->f);
+    if(rc)
+      return vr(rc);
+  }
+  return VK_SUCCESS;
+}
 
 VISOR_EXPORT void visor_gb300_set_mode(int mode) { g_mode = mode; }
 VISOR_EXPORT int visor_gb300_get_mode(void) { return default_mode(); }

@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "visor_gpu.h"
+#include "vgpu_noalloc.h"
 #include "../kernels/vgx_tiles.cuh"
 
 #include "vgx_sources.inc" /* generated: kVgxTypes, kVgxDevice, kVgxTiles, kVgxStage */
@@ -1472,5 +1473,246 @@ extern "C" int vgpu_queue_flush_l2(vgpu_queue *q)
   if(!q->flush)
     CK(cudaMalloc(&q->flush, bytes));
   CK(cudaMemsetAsync(q->flush, (int)(q->launches & 0xff), bytes, q->stream));
+  return VGPU_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* submission without device allocation                                      */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * Per-call binning storage of vgpu_submit_noalloc: (tile, triangle) key/value
+ * pairs and their sort ping-pong, per-tile ranges and work list, the radix
+ * histogram and its scan partials.  18.5 MiB, reserved when the module loads,
+ * shared by every call on a device (calls that overlap in time race on it).
+ */
+namespace
+{
+constexpr u32 kFixedPairs = 1u << 20; /* tile pairs per job */
+constexpr u32 kFixedTiles = 1u << 17; /* bin tiles per job */
+constexpr u64 kFixedHistWords = (u64)(kFixedPairs / kSortTile) * 256 + 256;
+constexpr u64 kFixedScanWords = 1024;
+constexpr u64 kFixedWords =
+    4ull * kFixedPairs + 3ull * kFixedTiles + kFixedHistWords + kFixedScanWords;
+constexpr int kFixedMaxDevices = 64;
+
+std::mutex g_fixed_mu;
+u32 *g_fixed_base[kFixedMaxDevices];
+
+struct FixedBufs
+{
+  u32 *keys[2], *vals[2];
+  u32 *tstart, *tend, *work;
+  u32 *hist, *scan;
+};
+}    // namespace
+
+static __device__ __align__(256) u32 g_fixed_scratch[kFixedWords];
+
+/* Device address of g_fixed_scratch on the current device, looked up once per
+   device (the first call on a device must not be inside a stream capture). */
+static int fixed_buffers(FixedBufs *b)
+{
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if(dev < 0 || dev >= kFixedMaxDevices)
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  u32 *base = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_fixed_mu);
+    if(!g_fixed_base[dev])
+    {
+      void *p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_fixed_scratch);
+      if(e != cudaSuccess || !p)
+      {
+        fprintf(stderr, "visor_gb300: cudaGetSymbolAddress(fixed scratch) failed on device %d: %s\n",
+                dev, cudaGetErrorString(e));
+        return VGPU_ERROR_INITIALIZATION_FAILED;
+      }
+      g_fixed_base[dev] = (u32 *)p;
+    }
+    base = g_fixed_base[dev];
+  }
+  u32 *p = base;
+  for(int i = 0; i < 2; i++)
+  {
+    b->keys[i] = p;
+    p += kFixedPairs;
+    b->vals[i] = p;
+    p += kFixedPairs;
+  }
+  b->tstart = p;
+  p += kFixedTiles;
+  b->tend = p;
+  p += kFixedTiles;
+  b->work = p;
+  p += kFixedTiles;
+  b->hist = p;
+  p += kFixedHistWords;
+  b->scan = p;
+  return VGPU_OK;
+}
+
+/* phase B of a job with every per-call buffer taken from the fixed scratch */
+static int run_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, const FixedBufs &b)
+{
+  Job &j = l->jobs[ji];
+  VgxJob J = make_job(q, l, j, ji);
+  J.keys = (u64)b.keys[0];
+  J.vals = (u64)b.vals[0];
+  J.keys_alt = (u64)b.keys[1];
+  J.vals_alt = (u64)b.vals[1];
+  J.tile_start = (u64)b.tstart;
+  J.tile_end = (u64)b.tend;
+  J.work = j.all_tiles ? 0 : (u64)b.work;
+  J.scratch = (u64)b.scan;
+  J.pair_capacity = kFixedPairs;
+  u32 *counts = l->d_counts + j.cnt_off;
+  const u32 total = l->h_totals[ji];
+  /* what the kernels expect to start at zero: pair total, work queue and count,
+     tile ranges (tiles without pairs keep an empty range) */
+  CK(cudaMemsetAsync(q->status + 1, 0, 12, q->stream));
+  if(j.all_tiles || total)
+  {
+    CK(cudaMemsetAsync(b.tstart, 0, (size_t)j.num_tiles * 4, q->stream));
+    CK(cudaMemsetAsync(b.tend, 0, (size_t)j.num_tiles * 4, q->stream));
+  }
+  q->stats.pairs += total;
+  int src = 0;
+  if(total)
+  {
+    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.prog->rec_words, counts);
+    q->launches++;
+    const u32 nb = (total + kSortTile - 1) / kSortTile;
+    const u64 n = (u64)nb * 256;
+    std::vector<u64> lv;
+    u64 need = 0;
+    for(u64 m = n; m > (u64)kScanTile;)
+    {
+      m = (m + kScanTile - 1) / kScanTile;
+      lv.push_back(need);
+      need += m + 1;
+    }
+    if(need + 4 > kFixedScanWords)
+      return VGPU_ERROR_OUT_OF_DEVICE_MEMORY;
+    for(u32 shift = 0; shift < j.key_bits; shift += 8)
+    {
+      k_radix_hist<<<nb, kSortBlock, 0, q->stream>>>(b.keys[src], total, shift, b.hist, nb);
+      int rc = scan_u32(q, b.hist, b.hist, n, b.scan, lv, 0);
+      if(rc)
+        return rc;
+      k_radix_scatter<<<nb, kSortBlock, 0, q->stream>>>(b.keys[src], b.vals[src], total, shift,
+                                                        b.hist, nb, b.keys[src ^ 1], b.vals[src ^ 1]);
+      q->launches += 2;
+      src ^= 1;
+    }
+    J.keys = (u64)b.keys[src];
+    J.vals = (u64)b.vals[src];
+    CK(cudaMemcpyAsync(q->status + 1, counts + j.num_tris, 4, cudaMemcpyDeviceToDevice, q->stream));
+    unsigned rg = std::min<u32>((total + 255) / 256, (u32)g_sms * 8);
+    k_ranges<<<rg, 256, 0, q->stream>>>(b.keys[src], q->status + 1, kFixedPairs, b.tstart, b.tend,
+                                        j.all_tiles ? nullptr : b.work, q->status);
+    q->launches++;
+  }
+  if(!j.all_tiles && !total)
+    return VGPU_OK;
+  const unsigned warps = j.var->warps;
+  const unsigned per_sm = g_tuning.raster_blocks_per_sm ? g_tuning.raster_blocks_per_sm
+                                                        : std::max(1u, 32u / warps);
+  unsigned grid = std::max(1u, (unsigned)g_sms * per_sm);
+  const u32 bins = j.all_tiles ? j.num_tiles : total;
+  grid = std::max(1u, std::min<unsigned>(grid, bins));
+  return launch(q, j.var->raster, grid, warps * 32, &J);
+}
+
+extern "C" int vgpu_submit_noalloc(vgpu_queue *q, vgpu_list *l)
+{
+  if(!l->built)
+  {
+    fprintf(stderr, "visor_gb300: allocation-free submit needs a command list that an ordinary "
+                    "submit has already built\n");
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  }
+  CK(cudaSetDevice(g_device));
+  FixedBufs b;
+  int rc = fixed_buffers(&b);
+  if(rc)
+    return rc;
+  for(const Job &j : l->jobs)
+    if(j.num_tiles > kFixedTiles)
+    {
+      fprintf(stderr, "visor_gb300: allocation-free submit: a job spans %u bin tiles, the fixed "
+                      "scratch holds %u\n", j.num_tiles, kFixedTiles);
+      return VGPU_ERROR_OUT_OF_DEVICE_MEMORY;
+    }
+  CK(cudaEventRecord(q->ev0, q->stream));
+  for(auto &u : l->uploads)
+    CK(cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, q->stream));
+  size_t p = 0;
+  while(p < l->plan.size())
+  {
+    size_t e = p;
+    while(e < l->plan.size() && l->plan[e].kind != Exec::E_SEGMENT_END &&
+          l->plan[e].kind != Exec::E_COPY)
+      e++;
+    bool any_job = false;
+    for(size_t i = p; i < e; i++)
+      if(l->plan[i].kind == Exec::E_JOB)
+      {
+        rc = run_setup(q, l, l->plan[i].index);
+        if(rc)
+          return rc;
+        any_job = true;
+      }
+    if(any_job)
+    {
+      CK(cudaMemcpyAsync(l->h_totals, l->d_totals, l->jobs.size() * 4, cudaMemcpyDeviceToHost,
+                         q->stream));
+      CK(cudaStreamSynchronize(q->stream));
+      for(size_t i = p; i < e; i++)
+        if(l->plan[i].kind == Exec::E_JOB && l->h_totals[l->plan[i].index] > kFixedPairs)
+        {
+          fprintf(stderr, "visor_gb300: allocation-free submit: a job needs %u tile pairs, the "
+                          "fixed scratch holds %u (earlier segments of this submit have run)\n",
+                  l->h_totals[l->plan[i].index], kFixedPairs);
+          return VGPU_ERROR_OUT_OF_DEVICE_MEMORY;
+        }
+    }
+    for(size_t i = p; i < e; i++)
+    {
+      const Exec &x = l->plan[i];
+      if(x.kind == Exec::E_CLEAR)
+      {
+        u64 n = (u64)x.target.width * x.target.height;
+        unsigned g = (unsigned)std::min<u64>((n + 255) / 256, (u64)g_sms * 16);
+        k_clear<<<std::max(g, 1u), 256, 0, q->stream>>>(x.target, x.color, x.depth);
+        q->launches++;
+      }
+      else if(x.kind == Exec::E_JOB)
+      {
+        rc = run_raster_fixed(q, l, x.index, b);
+        if(rc)
+          return rc;
+      }
+    }
+    if(e < l->plan.size() && l->plan[e].kind == Exec::E_COPY)
+    {
+      const Cmd &c = l->cmds[l->plan[e].index];
+      CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, q->stream));
+    }
+    p = e + 1;
+  }
+  for(auto &d : l->downloads)
+    CK(cudaMemcpyAsync(d.first, d.second.first, d.second.second, cudaMemcpyDeviceToHost, q->stream));
+  CK(cudaEventRecord(q->ev1, q->stream));
+  q->rev_used = 0;
+  q->timed = true;
+  q->stats.tris_in += l->tris_in;
+  for(const Cmd &c : l->cmds)
+    if(c.type == CMD_DRAW)
+      q->stats.draws++;
+  q->stats.jobs += l->jobs.size();
+  CK(cudaGetLastError());
   return VGPU_OK;
 }

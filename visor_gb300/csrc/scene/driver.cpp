@@ -783,3 +783,5 @@ extern "C" void vsd_release(vsd_scene *s)
 }
 
 extern "C" void *vsd_queue(vsd_context *c) { return (void *)c->queue; }
+
+extern "C" void *vsd_command_buffer(vsd_scene *s) { return (void *)s->cmd; }
