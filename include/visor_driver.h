@@ -65,6 +65,12 @@ void *vsd_queue(vsd_context *ctx);
 /* The VkCommandBuffer the scene recorded (for callers that submit it themselves). */
 void *vsd_command_buffer(vsd_scene *s);
 
+/* Fill a serving request (visor_gb300_request of visor_icd.h) for draw `draw`
+   of the scene: its pipeline, descriptor set, vertex/index buffers, push
+   constants, target size and clear values.  Outputs and tag are left NULL/0.
+   Returns 0, or -1 when the draw does not exist. */
+int vsd_request(vsd_scene *s, uint32_t draw, void *request);
+
 /* Bytes copied host->device per submit when VSD_RESTAGE_INPUTS is set. */
 uint64_t vsd_restage_bytes(const vsd_scene *s);
 

@@ -127,6 +127,76 @@ typedef struct vgpu_tuning {
 void vgpu_set_tuning(const vgpu_tuning *t);
 void vgpu_get_tuning(vgpu_tuning *t);
 
+/*
+ * Serving engine: a request loop with continuous batching.
+ *
+ * A request renders one frame (one draw into its own colour + depth target of
+ * width x height, cleared first) from resources that stay resident on the
+ * device (programs, vertex/index buffers, textures).  vgpu_server_submit only
+ * enqueues.  A scheduler thread admits requests in arrival order while their
+ * device bytes fit the budget, and whenever one of `slots` streams is free it
+ * launches every admitted request (up to max_batch / max_batch_tris) as one
+ * batched list: the draws of one program merge into one job across the batch's
+ * targets.  Batches on different slots overlap on the device; requests that
+ * arrive meanwhile wait for the next free slot.  Per-batch storage (targets,
+ * triangle records, scans) is stream-ordered from a memory pool, so neither
+ * admission nor completion synchronises the device.  A request's result equals
+ * its rendering alone: batches never share targets, and within a job each
+ * tile sees its own target's triangles in primitive order.
+ */
+typedef struct vgpu_server vgpu_server;
+
+typedef struct vgpu_server_config {
+  uint64_t budget_bytes;   /* device bytes for admitted requests plus slot binning storage */
+  uint32_t slots;          /* batches in flight (one stream each); 0: 3 */
+  uint32_t max_batch;      /* requests per batch; 0: 64 */
+  uint64_t max_batch_tris; /* triangles per batch; 0: 16M */
+  uint64_t binning_pairs;  /* tile pairs each slot reserves at creation; 0: 8M */
+} vgpu_server_config;
+
+typedef struct vgpu_request {
+  vgpu_program *program;
+  VgxDraw draw;          /* resident buffers, state, push constants; target and tri_base are set by the server */
+  uint32_t width, height;
+  uint32_t clear_bgra;   /* clear colour as stored bytes */
+  float clear_depth;
+  void *out_color;       /* host memory for width*height*4 BGRA bytes, or NULL (pinned: asynchronous copy) */
+  float *out_depth;      /* host memory for width*height floats, or NULL */
+  uint64_t tag;          /* returned in the completion */
+  uint64_t arrival_ns;   /* vgpu_now_ns() time the request arrived; 0: now */
+} vgpu_request;
+
+typedef struct vgpu_completion {
+  uint64_t ticket, tag;
+  int32_t status;        /* VGPU_OK, or VGPU_ERROR_OUT_OF_DEVICE_MEMORY when the request alone exceeds the budget */
+  uint32_t batch_size;   /* requests in the batch it ran in */
+  uint64_t arrival_ns, admit_ns, done_ns; /* vgpu_now_ns() clock */
+} vgpu_completion;
+
+typedef struct vgpu_server_stats {
+  uint64_t submitted, completed, rejected, batches;
+  uint64_t reserved_bytes, peak_reserved_bytes; /* admitted requests' bytes (current, peak) */
+  uint64_t binning_bytes;                       /* slots' binning storage */
+  uint32_t max_batch_seen, in_flight;
+  uint64_t tris, shaded;                        /* over completed batches */
+} vgpu_server_stats;
+
+int vgpu_server_create(const vgpu_server_config *cfg, vgpu_server **out);
+/* Enqueue; never blocks on the device.  *ticket identifies the completion. */
+int vgpu_server_submit(vgpu_server *s, const vgpu_request *r, uint64_t *ticket);
+/* Move up to max finished requests into out; returns how many. */
+uint32_t vgpu_server_poll(vgpu_server *s, vgpu_completion *out, uint32_t max);
+/* Wait until nothing is queued or in flight (VGPU_TIMEOUT after timeout_ns). */
+int vgpu_server_wait(vgpu_server *s, uint64_t timeout_ns);
+int vgpu_server_stats_get(vgpu_server *s, vgpu_server_stats *out);
+/* Finish in-flight batches, fail queued requests, release everything. */
+void vgpu_server_destroy(vgpu_server *s);
+/* Monotonic clock of the serving timestamps (nanoseconds). */
+uint64_t vgpu_now_ns(void);
+/* Pinned host memory (for request outputs). */
+int vgpu_host_alloc(uint64_t bytes, void **out);
+void vgpu_host_free(void *p);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -77,6 +77,42 @@ int visor_gb300_flush_l2(VkQueue queue);
 VkResult visor_gb300_queue_submit_noalloc(VkQueue queue, uint32_t submitCount,
                                           const VkSubmitInfo *pSubmits, VkFence fence);
 
+/*
+ * Serving (no counterpart in the reference): a request loop with continuous
+ * batching over resources that stay resident (pipelines, vertex/index buffers,
+ * descriptor sets).  A request renders one draw into a new colour + depth
+ * target of width x height, cleared to clear_color / clear_depth, and copies
+ * the result to out_color (BGRA8) / out_depth when given.  Resident buffers and
+ * images must be device-local, or host-visible ones that a vkQueueSubmit has
+ * already uploaded.  Completion, waiting, statistics and destruction use the
+ * vgpu_server_* calls of visor_gpu.h on the returned server.
+ */
+typedef struct visor_gb300_request {
+  VkPipeline pipeline;
+  VkDescriptorSet set;             /* bound as set 0, or VK_NULL_HANDLE */
+  VkBuffer vertex_buffer;          /* binding 0 */
+  VkDeviceSize vertex_offset;
+  VkBuffer index_buffer;           /* VK_NULL_HANDLE: vkCmdDraw semantics */
+  VkDeviceSize index_offset;
+  VkIndexType index_type;
+  uint32_t count;                  /* index count (indexed) or vertex count */
+  uint32_t first;                  /* first index or first vertex */
+  uint32_t push_size;
+  uint8_t push[128];               /* push constants from offset 0 */
+  uint32_t width, height;
+  float clear_color[4];
+  float clear_depth;
+  void *out_color;                 /* width*height*4 bytes (pinned host memory: asynchronous copy), or NULL */
+  float *out_depth;                /* width*height floats, or NULL */
+  uint64_t tag;
+  uint64_t arrival_ns;             /* vgpu_now_ns() clock; 0 = now */
+} visor_gb300_request;
+
+VkResult visor_gb300_server_create(VkDevice device, const vgpu_server_config *config,
+                                   vgpu_server **server);
+VkResult visor_gb300_server_submit(vgpu_server *server, const visor_gb300_request *request,
+                                   uint64_t *ticket);
+
 /* SPIR-V pair -> CUDA source, without a device (returns 0 and err on failure). */
 size_t visor_gb300_translate(const uint32_t *vs_words, size_t vs_count, const uint32_t *fs_words,
                              size_t fs_count, char *out, size_t size, char *err, size_t err_size);

@@ -1,0 +1,227 @@
+"""Serving loop: continuous batching of render requests (configuration 5 shapes).
+
+Each request is the one draw of a seeded serving scene (a procedural sphere
+mesh, a mipmapped texture sampled trilinearly, its own MVP and resolution).
+The scenes are uploaded once and stay resident; the server renders requests
+into targets it allocates from its budget.  Every served frame must equal, bit
+for bit, the frame vkQueueSubmit renders for the same scene alone, whether the
+request ran alone or mixed with others arriving at random times, and whatever
+the budget and slot count.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+import visor_gb300 as vg
+from visor_gb300 import scene as vs
+from visor_gb300 import serve
+
+SEED = 77
+N_REQ = 12
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors have the C layout of include/visor_icd.h / visor_gpu.h."""
+    checks = {
+        "visor_gb300_request": serve.Request, "vgpu_completion": serve.Completion,
+        "vgpu_server_config": serve.ServerConfig, "vgpu_server_stats": serve.ServerStats,
+    }
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "visor_icd.h"', "int main(void) {"]
+    for cname, py in checks.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for cname, py in checks.items():
+        import ctypes
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+gpu = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def device():
+    d = vg.Device()
+    yield d
+    d.close()
+
+
+def _scene(lib, index, **kw):
+    params = dict(count=index, max_tris=120000, textures=4, tex_size=256)
+    params.update(kw)
+    return vs.generate(lib, vs.CFG_SERVING, SEED, **params)
+
+
+@pytest.fixture(scope="module")
+def pool(device):
+    """Resident request scenes with the frame vkQueueSubmit gives each alone."""
+    items = []
+    for i in range(N_REQ):
+        h = _scene(device.lib, i)
+        up = device.upload(h)
+        up.submit()
+        cols, deps = up.read()
+        items.append({"handle": h, "up": up, "color": cols[0].copy(), "depth": deps[0].copy(),
+                      "w": h.s.targets[0].width, "h": h.s.targets[0].height})
+    yield items
+    for it in items:
+        it["up"].release()
+
+
+class Outputs:
+    """Pinned host buffers for the results of a set of requests."""
+
+    def __init__(self, items):
+        self.bufs = []
+        for it in items:
+            px = it["w"] * it["h"]
+            b = serve.PinnedBuffer(px * 8)
+            b.view(np.uint8, px * 8)[:] = 0xAB
+            self.bufs.append((b, px))
+
+    def addresses(self, i):
+        b, px = self.bufs[i]
+        return b.ptr, b.ptr + px * 4
+
+    def frame(self, i):
+        b, px = self.bufs[i]
+        return b.view(np.uint8, px * 4).copy(), b.view(np.float32, px, px * 4).copy()
+
+    def free(self):
+        for b, _ in self.bufs:
+            b.free()
+
+
+def _serve(device, pool, order, budget=4 << 30, slots=3, arrivals_s=None, binning_pairs=1 << 20,
+           max_batch=0):
+    srv = serve.Server(device, budget, slots=slots, binning_pairs=binning_pairs, max_batch=max_batch)
+    outs = Outputs([pool[i] for i in order])
+    try:
+        t0 = serve.now_ns()
+        for k, i in enumerate(order):
+            if arrivals_s is not None:
+                due = t0 + int(arrivals_s[k] * 1e9)
+                while serve.now_ns() < due:
+                    pass
+            col, dep = outs.addresses(k)
+            srv.submit(serve.request_for(pool[i]["up"]), out_color=col, out_depth=dep, tag=k)
+        assert srv.wait(timeout_s=120)
+        done = srv.poll(1024)
+        stats = srv.stats()
+        frames = [outs.frame(k) for k in range(len(order))]
+    finally:
+        srv.close()
+        outs.free()
+    return frames, sorted(done, key=lambda c: c["tag"]), stats
+
+
+def _assert_frame(pool_item, frame, what):
+    col, dep = frame
+    assert np.array_equal(col, pool_item["color"].reshape(-1)), what
+    assert np.array_equal(dep.view(np.uint32), pool_item["depth"].reshape(-1).view(np.uint32)), what
+
+
+@gpu
+def test_served_frames_equal_queue_submit(device, pool):
+    order = list(range(N_REQ))
+    frames, done, stats = _serve(device, pool, order, slots=1)
+    assert [c["status"] for c in done] == [0] * N_REQ
+    for k, i in enumerate(order):
+        _assert_frame(pool[i], frames[k], f"request {i}")
+    assert stats["completed"] == N_REQ and stats["rejected"] == 0
+    # a burst into one slot: everything queued behind the first batch runs together
+    assert stats["batches"] <= 3 and stats["max_batch_seen"] >= 4, stats
+    assert stats["shaded"] > 0
+
+
+@gpu
+def test_alone_equals_mixed(device, pool):
+    alone, done_a, _ = _serve(device, pool, [5])
+    assert done_a[0]["status"] == 0
+    rng = np.random.default_rng(3)
+    order = list(rng.permutation(N_REQ)) + [5, 5]
+    arrivals = np.cumsum(rng.exponential(1.0 / 2000.0, size=len(order)))
+    mixed, done_m, stats = _serve(device, pool, order, arrivals_s=arrivals)
+    assert all(c["status"] == 0 for c in done_m)
+    for k, i in enumerate(order):
+        _assert_frame(pool[i], mixed[k], f"mixed position {k} (request {i})")
+        if i == 5:
+            assert np.array_equal(mixed[k][0], alone[0][0])
+            assert np.array_equal(mixed[k][1].view(np.uint32), alone[0][1].view(np.uint32))
+
+
+@gpu
+def test_budget_bounds_admission(device, pool):
+    probe = serve.Server(device, 4 << 30, slots=2, binning_pairs=1 << 20)
+    binning = probe.stats()["binning_bytes"]
+    probe.close()
+    # room for about one large request at a time (upper bound of a request's bytes)
+    worst = max(it["w"] * it["h"] * 8 + it["handle"].s.draws[0].count // 3 * 480 + (1 << 16) for it in pool)
+    budget = binning + int(worst * 1.5)
+    order = list(range(N_REQ))
+    frames, done, stats = _serve(device, pool, order, budget=budget, slots=2)
+    assert all(c["status"] == 0 for c in done)
+    assert stats["peak_reserved_bytes"] <= budget - stats["binning_bytes"]
+    for k, i in enumerate(order):
+        _assert_frame(pool[i], frames[k], f"request {i}")
+
+
+@gpu
+def test_request_over_budget_is_rejected(device):
+    small = _scene(device.lib, 1, width=256, height=256, min_tris=1000, max_tris=2000)
+    big = _scene(device.lib, 2, width=1024, height=1024, min_tris=1000, max_tris=2000)
+    ups = [device.upload(small), device.upload(big)]
+    try:
+        for up in ups:
+            up.submit()
+        want = ups[0].read()
+        probe = serve.Server(device, 4 << 30, slots=1, binning_pairs=1 << 20)
+        binning = probe.stats()["binning_bytes"]
+        probe.close()
+        srv = serve.Server(device, binning + (3 << 20), slots=1, binning_pairs=1 << 20)
+        out = serve.PinnedBuffer(256 * 256 * 8)
+        try:
+            srv.submit(serve.request_for(ups[1]), tag=1)
+            srv.submit(serve.request_for(ups[0]), out_color=out.ptr, out_depth=out.ptr + 256 * 256 * 4, tag=0)
+            assert srv.wait(timeout_s=60)
+            done = {c["tag"]: c for c in srv.poll()}
+            assert done[1]["status"] == -2  # VK_ERROR_OUT_OF_DEVICE_MEMORY: 1024x1024 targets alone exceed it
+            assert done[0]["status"] == 0
+            assert np.array_equal(out.view(np.uint8, 256 * 256 * 4), want[0][0].reshape(-1))
+        finally:
+            srv.close()
+            out.free()
+    finally:
+        for up in ups:
+            up.release()
+
+
+@gpu
+def test_served_frame_equals_oracle(device):
+    from oracle import loader
+    h = _scene(device.lib, 4, width=256, height=256, min_tris=2000, max_tris=5000)
+    up = device.upload(h)
+    try:
+        up.submit()
+        item = {"up": up, "w": 256, "h": 256}
+        frames, done, _ = _serve(device, [item], [0])
+        assert done[0]["status"] == 0
+        cols, deps, _ = loader.Oracle().render(h)
+        assert np.array_equal(frames[0][0], cols[0].reshape(-1))
+        assert np.array_equal(frames[0][1].view(np.uint32), deps[0].reshape(-1).view(np.uint32))
+    finally:
+        up.release()

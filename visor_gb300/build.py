@@ -30,7 +30,7 @@ KERNEL_SOURCES = [
 ]
 
 C_SOURCES = ["scene/scene.c", "scene/spirv_emit.c"]
-CXX_SOURCES = ["icd/icd.cpp", "spirv/translate.cpp", "scene/driver.cpp"]
+CXX_SOURCES = ["icd/icd.cpp", "spirv/translate.cpp", "scene/driver.cpp", "runtime/serve.cpp"]
 CU_SOURCES = ["runtime/vgpu.cu"]
 
 

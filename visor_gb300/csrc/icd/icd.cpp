@@ -1250,6 +1250,62 @@ void fill_texture(VgxTex &t, VkDescriptorSet_T::Bind *b)
   }
 }
 
+/* Pipeline state, vertex attributes, sampled images and uniform buffers of a
+   draw of `count` vertices/indices with descriptor sets `sets` bound
+   (cmd_exec.cpp:129-142 binds the same state at draw time); `note` sees every
+   memory object the draw reads. */
+template <class Note>
+void fill_draw_state(VgxDraw &d, VkPipeline_T *p, VkDescriptorSet_T *const *sets, uint32_t count,
+                     Note note)
+{
+  d.topology = p->topology == 4 ? VGX_TOPO_STRIP : VGX_TOPO_LIST;
+  d.num_tris = d.topology == VGX_TOPO_STRIP ? (count >= 3 ? count - 2 : 0) : count / 3;
+  d.cull_mode = p->cull;
+  d.front_face = p->front;
+  d.depth_op = p->depth_op;
+  d.depth_write = p->depth_write;
+  d.blend_enable = p->blend;
+  d.src_factor = p->src;
+  d.dst_factor = p->dst;
+  d.blend_op = p->op;
+  for(int a = 0; a < VGX_MAX_ATTRS; a++)
+  {
+    d.attrs[a].format = p->attrs[a].format;
+    d.attrs[a].binding = p->attrs[a].binding;
+    d.attrs[a].offset = p->attrs[a].offset;
+    d.attrs[a].stride = p->strides[p->attrs[a].binding];
+  }
+  for(size_t t = 0; t < p->tr.textures.size() && t < VGX_MAX_TEX; t++)
+  {
+    const vst::Binding &bd = p->tr.textures[t];
+    VkDescriptorSet_T *set = bd.set < 8 ? sets[bd.set] : nullptr;
+    VkDescriptorSet_T::Bind *bind = nullptr;
+    if(set)
+    {
+      auto it = set->binds.find(bd.binding);
+      if(it != set->binds.end())
+        bind = &it->second;
+    }
+    fill_texture(d.tex[t], bind);
+    if(bind && bind->view && bind->view->image)
+      note(bind->view->image->mem);
+  }
+  for(size_t u = 0; u < p->tr.ubos.size() && u < VGX_MAX_UBO; u++)
+  {
+    const vst::Binding &bd = p->tr.ubos[u];
+    VkDescriptorSet_T *set = bd.set < 8 ? sets[bd.set] : nullptr;
+    if(!set)
+      continue;
+    auto it = set->binds.find(bd.binding);
+    if(it != set->binds.end() && it->second.buffer && it->second.buffer->mem)
+    {
+      VkBuffer_T *ub = it->second.buffer;
+      d.ubo[u] = (u64)dev_addr(ub->mem, ub->offset + it->second.offset);
+      note(ub->mem);
+    }
+  }
+}
+
 /* Replay the packet stream into a vgpu list (cmd_exec.cpp:15-185). */
 void lower(VkCommandBuffer c)
 {
@@ -1406,52 +1462,7 @@ void lower(VkCommandBuffer c)
           d.index_type = VGX_INDEX_NONE;
         }
         d.first = b.first;
-        d.topology = p->topology == 4 ? VGX_TOPO_STRIP : VGX_TOPO_LIST;
-        d.num_tris = d.topology == VGX_TOPO_STRIP ? (b.count >= 3 ? b.count - 2 : 0) : b.count / 3;
-        d.cull_mode = p->cull;
-        d.front_face = p->front;
-        d.depth_op = p->depth_op;
-        d.depth_write = p->depth_write;
-        d.blend_enable = p->blend;
-        d.src_factor = p->src;
-        d.dst_factor = p->dst;
-        d.blend_op = p->op;
-        for(int a = 0; a < VGX_MAX_ATTRS; a++)
-        {
-          d.attrs[a].format = p->attrs[a].format;
-          d.attrs[a].binding = p->attrs[a].binding;
-          d.attrs[a].offset = p->attrs[a].offset;
-          d.attrs[a].stride = p->strides[p->attrs[a].binding];
-        }
-        for(size_t t = 0; t < p->tr.textures.size() && t < VGX_MAX_TEX; t++)
-        {
-          const vst::Binding &bd = p->tr.textures[t];
-          VkDescriptorSet_T *set = bd.set < 8 ? s.sets[bd.set] : nullptr;
-          VkDescriptorSet_T::Bind *bind = nullptr;
-          if(set)
-          {
-            auto it = set->binds.find(bd.binding);
-            if(it != set->binds.end())
-              bind = &it->second;
-          }
-          fill_texture(d.tex[t], bind);
-          if(bind && bind->view && bind->view->image)
-            note_read(use, bind->view->image->mem);
-        }
-        for(size_t u = 0; u < p->tr.ubos.size() && u < VGX_MAX_UBO; u++)
-        {
-          const vst::Binding &bd = p->tr.ubos[u];
-          VkDescriptorSet_T *set = bd.set < 8 ? s.sets[bd.set] : nullptr;
-          if(!set)
-            continue;
-          auto it = set->binds.find(bd.binding);
-          if(it != set->binds.end() && it->second.buffer && it->second.buffer->mem)
-          {
-            VkBuffer_T *ub = it->second.buffer;
-            d.ubo[u] = (u64)dev_addr(ub->mem, ub->offset + it->second.offset);
-            note_read(use, ub->mem);
-          }
-        }
+        fill_draw_state(d, p, s.sets, b.count, [&](VkDeviceMemory_T *m) { note_read(use, m); });
         memcpy(d.push, s.push, 128);
         if(d.num_tris)
           vgpu_list_draw(l, p->prog, &d, &s.target);
@@ -1647,6 +1658,56 @@ VISOR_EXPORT VkResult visor_gb300_queue_submit_noalloc(VkQueue q, uint32_t n,
       return vr(rc);
   }
   return VK_SUCCESS;
+}
+
+VISOR_EXPORT VkResult visor_gb300_server_create(VkDevice device, const vgpu_server_config *config,
+                                                vgpu_server **server)
+{
+  (void)device;
+  return vr(vgpu_server_create(config, server));
+}
+
+/* A request becomes the VgxDraw that lowering a one-draw render pass would give. */
+VISOR_EXPORT VkResult visor_gb300_server_submit(vgpu_server *server, const visor_gb300_request *r,
+                                                uint64_t *ticket)
+{
+  VkPipeline_T *p = r->pipeline;
+  VkBuffer_T *vb = r->vertex_buffer;
+  if(!p || !p->prog || !vb || !vb->mem || r->push_size > 128)
+    return VK_ERROR_INITIALIZATION_FAILED;
+  vgpu_request q;
+  memset(&q, 0, sizeof(q));
+  q.program = p->prog;
+  VgxDraw &d = q.draw;
+  d.vb[0] = (u64)dev_addr(vb->mem, vb->offset + r->vertex_offset);
+  d.vb_bytes[0] = vb->size > r->vertex_offset ? vb->size - r->vertex_offset : 0;
+  VkBuffer_T *ib = r->index_buffer;
+  if(ib && ib->mem)
+  {
+    const uint32_t isz = r->index_type == VK_INDEX_TYPE_UINT16 ? 2 : 4;
+    d.ib = (u64)dev_addr(ib->mem, ib->offset + r->index_offset);
+    d.ib_count = ib->size > r->index_offset ? (ib->size - r->index_offset) / isz : 0;
+    d.index_type = r->index_type == VK_INDEX_TYPE_UINT16 ? VGX_INDEX_U16 : VGX_INDEX_U32;
+  }
+  else
+  {
+    d.index_type = VGX_INDEX_NONE;
+  }
+  d.first = r->first;
+  VkDescriptorSet_T *sets[8] = {r->set};
+  fill_draw_state(d, p, sets, r->count, [](VkDeviceMemory_T *) {});
+  memcpy(d.push, r->push, r->push_size);
+  VkClearColorValue cc;
+  memcpy(cc.float32, r->clear_color, sizeof(cc.float32));
+  q.width = r->width;
+  q.height = r->height;
+  q.clear_bgra = clear_bgra(cc);
+  q.clear_depth = r->clear_depth;
+  q.out_color = r->out_color;
+  q.out_depth = r->out_depth;
+  q.tag = r->tag;
+  q.arrival_ns = r->arrival_ns;
+  return vr(vgpu_server_submit(server, &q, ticket));
 }
 
 VISOR_EXPORT void visor_gb300_set_mode(int mode) { g_mode = mode; }

@@ -1,0 +1,542 @@
+/*
+ * serve.cpp - serving engine: a request loop with continuous batching.
+ *
+ * Requests (one draw into a fresh target each, over resident buffers and
+ * textures) are queued by vgpu_server_submit.  One scheduler thread owns the
+ * device work.  Each slot is a vgpu_queue with its own stream and binning
+ * storage; a slot runs one batch at a time in two stages:
+ *
+ *   stage 1  targets + list storage allocated from the server's memory pool in
+ *            stream order, triangle setup and tile-count scans of every job,
+ *            pair totals copied to pinned host memory;
+ *   stage 2  (after stage 1 completes) binning storage sized, clears fused into
+ *            the raster, binning, raster, result downloads, stream-ordered frees.
+ *
+ * The end of each stage is signalled by a host function on the slot's stream,
+ * so the scheduler never blocks on the device: while one slot rasterises,
+ * another runs setup and a third waits for arrivals.  Admission is in arrival
+ * order against a device-byte budget (a request's target, triangle records and
+ * scans, plus every slot's binning storage); a request that cannot fit even
+ * into an idle server is rejected with VGPU_ERROR_OUT_OF_DEVICE_MEMORY.
+ *
+ * The reference has no serving loop (its vkQueueSubmit renders one command
+ * buffer synchronously on the calling thread, cmd_exec.cpp:187-201).
+ */
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include <time.h>
+
+#include <algorithm>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "visor_gpu.h"
+#include "vgpu_internal.h"
+
+namespace
+{
+constexpr uint32_t kDefaultSlots = 3;
+constexpr uint32_t kDefaultMaxBatch = 64;
+constexpr uint64_t kDefaultMaxBatchTris = 16ull << 20;
+constexpr uint64_t kDefaultBinningPairs = 8ull << 20;
+constexpr uint32_t kMaxTargetEdge = 16384;
+
+uint64_t align256(uint64_t v) { return (v + 255) & ~255ull; }
+
+struct Req
+{
+  uint64_t ticket = 0;
+  vgpu_request r;
+  uint64_t need = 0;     /* device bytes reserved while admitted */
+  uint64_t tris = 0;
+  uint64_t admit_ns = 0;
+  void *dmem = nullptr;  /* colour then depth */
+};
+
+struct Slot
+{
+  vgpu_server *srv = nullptr;
+  vgpu_queue *q = nullptr;
+  cudaStream_t stream = nullptr;
+  uint32_t *h_totals = nullptr; /* pinned, one word per job */
+  size_t cap = 0;
+  int stage = 0;                /* 0 free, 1 setup queued, 2 raster queued */
+  bool signalled = false;       /* guarded by vgpu_server::ev_mu */
+  std::vector<Req *> reqs;
+  vgpu_list *list = nullptr;
+  uint64_t shaded_seen = 0;
+};
+}    // namespace
+
+struct vgpu_server
+{
+  vgpu_server_config cfg;
+  int device = 0;
+  cudaMemPool_t pool = nullptr;
+  std::vector<Slot> slots;
+  std::thread th;
+
+  std::mutex mu; /* pending, done, accounting */
+  std::condition_variable idle_cv;
+  std::deque<Req *> pending;
+  std::deque<vgpu_completion> done;
+  uint64_t next_ticket = 1;
+  uint64_t reserved = 0, binning = 0, in_flight = 0;
+  vgpu_server_stats stats;
+
+  std::mutex ev_mu; /* slot signals and wake-ups */
+  std::condition_variable ev_cv;
+  bool wake = false, stop = false;
+};
+
+extern "C" uint64_t vgpu_now_ns(void)
+{
+  timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (uint64_t)ts.tv_sec * 1000000000ull + (uint64_t)ts.tv_nsec;
+}
+
+extern "C" int vgpu_host_alloc(uint64_t bytes, void **out)
+{
+  int rc = vgpu_init();
+  if(rc)
+    return rc;
+  if(cudaMallocHost(out, bytes ? bytes : 1) != cudaSuccess)
+  {
+    cudaGetLastError();
+    *out = nullptr;
+    return VGPU_ERROR_OUT_OF_HOST_MEMORY;
+  }
+  return VGPU_OK;
+}
+
+extern "C" void vgpu_host_free(void *p)
+{
+  if(p)
+    cudaFreeHost(p);
+}
+
+namespace
+{
+void CUDART_CB on_stage_end(void *p)
+{
+  /* runs on a CUDA callback thread: no CUDA calls here */
+  Slot *s = (Slot *)p;
+  {
+    std::lock_guard<std::mutex> g(s->srv->ev_mu);
+    s->signalled = true;
+    s->srv->wake = true;
+  }
+  s->srv->ev_cv.notify_one();
+}
+
+void wake(vgpu_server *S)
+{
+  {
+    std::lock_guard<std::mutex> g(S->ev_mu);
+    S->wake = true;
+  }
+  S->ev_cv.notify_one();
+}
+
+/* Complete requests (under S->mu) and release their reservations. */
+void complete_locked(vgpu_server *S, std::vector<Req *> &reqs, int status, uint64_t t,
+                     bool was_admitted)
+{
+  for(Req *r : reqs)
+  {
+    vgpu_completion c;
+    memset(&c, 0, sizeof(c));
+    c.ticket = r->ticket;
+    c.tag = r->r.tag;
+    c.status = status;
+    c.batch_size = (uint32_t)reqs.size();
+    c.arrival_ns = r->r.arrival_ns;
+    c.admit_ns = r->admit_ns;
+    c.done_ns = t;
+    S->done.push_back(c);
+    if(was_admitted)
+    {
+      S->reserved -= r->need;
+      S->in_flight--;
+    }
+    if(status == VGPU_OK)
+    {
+      S->stats.completed++;
+      S->stats.tris += r->tris;
+    }
+    else
+    {
+      S->stats.rejected++;
+    }
+    delete r;
+  }
+  reqs.clear();
+  S->idle_cv.notify_all();
+}
+
+void fail_batch(vgpu_server *S, Slot &sl, int rc)
+{
+  /* the stream may still hold work that uses the batch's memory: drain first */
+  cudaStreamSynchronize(sl.stream);
+  cudaGetLastError();
+  for(Req *r : sl.reqs)
+    if(r->dmem)
+      cudaFreeAsync(r->dmem, sl.stream);
+  if(sl.list)
+    vgpu_list_destroy_pooled(sl.list);
+  sl.list = nullptr;
+  cudaStreamSynchronize(sl.stream);
+  std::lock_guard<std::mutex> g(S->mu);
+  complete_locked(S, sl.reqs, rc, vgpu_now_ns(), true);
+  sl.stage = 0;
+}
+
+/* Stage 1 finished on the device: queue stage 2. */
+void start_raster(vgpu_server *S, Slot &sl)
+{
+  int rc = vgpu_list_phase_b(sl.q, sl.list);
+  if(rc)
+  {
+    fail_batch(S, sl, rc);
+    return;
+  }
+  for(Req *r : sl.reqs)
+  {
+    cudaFreeAsync(r->dmem, sl.stream);
+    r->dmem = nullptr;
+  }
+  vgpu_list_destroy_pooled(sl.list);
+  sl.list = nullptr;
+  if(cudaLaunchHostFunc(sl.stream, on_stage_end, &sl) != cudaSuccess)
+  {
+    fail_batch(S, sl, VGPU_ERROR_DEVICE_LOST);
+    return;
+  }
+  sl.stage = 2;
+  uint64_t b = 0;
+  for(Slot &o : S->slots)
+    b += vgpu_queue_binning_bytes(o.q);
+  std::lock_guard<std::mutex> g(S->mu);
+  S->binning = b;
+  S->stats.binning_bytes = b;
+}
+
+/* Stage 2 finished: the batch's results are in host memory. */
+void finish_batch(vgpu_server *S, Slot &sl)
+{
+  const uint64_t t = vgpu_now_ns();
+  vgpu_stats st;
+  int rc = vgpu_queue_stats(sl.q, &st);
+  uint64_t shaded = 0;
+  if(rc == VGPU_OK)
+  {
+    shaded = st.shaded - sl.shaded_seen;
+    sl.shaded_seen = st.shaded;
+    if(st.status)
+    {
+      /* an index outside its buffer (or a sizing fault): fail this batch, clear the sticky bits */
+      rc = VGPU_ERROR_DEVICE_LOST;
+      vgpu_queue_reset_stats(sl.q);
+      sl.shaded_seen = 0;
+    }
+  }
+  std::lock_guard<std::mutex> g(S->mu);
+  S->stats.shaded += shaded;
+  S->stats.batches++;
+  complete_locked(S, sl.reqs, rc, t, true);
+  sl.stage = 0;
+}
+
+/* Admit queued requests into a free slot and queue stage 1. */
+void launch_batch(vgpu_server *S, Slot &sl)
+{
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    uint64_t tris = 0;
+    const uint64_t room = S->cfg.budget_bytes > S->binning ? S->cfg.budget_bytes - S->binning : 0;
+    while(!S->pending.empty() && sl.reqs.size() < S->cfg.max_batch)
+    {
+      Req *r = S->pending.front();
+      if(r->need > room)
+      {
+        S->pending.pop_front();
+        std::vector<Req *> one{r};
+        fprintf(stderr, "visor_gb300: serving request %llu needs %llu device bytes, budget leaves %llu\n",
+                (unsigned long long)r->ticket, (unsigned long long)r->need,
+                (unsigned long long)room);
+        complete_locked(S, one, VGPU_ERROR_OUT_OF_DEVICE_MEMORY, vgpu_now_ns(), false);
+        continue;
+      }
+      if(S->reserved + r->need > room)
+        break; /* wait for memory: admission stays in arrival order */
+      if(!sl.reqs.empty() && tris + r->tris > S->cfg.max_batch_tris)
+        break;
+      S->pending.pop_front();
+      S->reserved += r->need;
+      S->in_flight++;
+      S->stats.peak_reserved_bytes = std::max(S->stats.peak_reserved_bytes, S->reserved);
+      r->admit_ns = vgpu_now_ns();
+      tris += r->tris;
+      sl.reqs.push_back(r);
+    }
+    if(sl.reqs.empty())
+      return;
+    S->stats.max_batch_seen = std::max<uint32_t>(S->stats.max_batch_seen, (uint32_t)sl.reqs.size());
+  }
+  int rc = VGPU_OK;
+  sl.list = vgpu_list_create();
+  vgpu_list_set_mode(sl.list, VGPU_MODE_BATCHED);
+  for(Req *r : sl.reqs)
+  {
+    const uint64_t px = (uint64_t)r->r.width * r->r.height;
+    if(cudaMallocFromPoolAsync(&r->dmem, align256(px * 4) + px * 4, S->pool, sl.stream) != cudaSuccess)
+    {
+      cudaGetLastError();
+      r->dmem = nullptr;
+      rc = VGPU_ERROR_OUT_OF_DEVICE_MEMORY;
+      break;
+    }
+    VgxTarget t;
+    memset(&t, 0, sizeof(t));
+    t.color = (uint64_t)r->dmem;
+    t.depth = (uint64_t)r->dmem + align256(px * 4);
+    t.width = (int32_t)r->r.width;
+    t.height = (int32_t)r->r.height;
+    t.clear_bgra = r->r.clear_bgra;
+    t.clear_depth = r->r.clear_depth;
+    vgpu_list_clear(sl.list, &t, 1, 1);
+    vgpu_list_draw(sl.list, r->r.program, &r->r.draw, &t);
+    if(r->r.out_color)
+      vgpu_list_download(sl.list, r->r.out_color, (void *)t.color, px * 4);
+    if(r->r.out_depth)
+      vgpu_list_download(sl.list, r->r.out_depth, (void *)t.depth, px * 4);
+  }
+  if(rc == VGPU_OK)
+    rc = vgpu_list_build_pooled(sl.list, S->pool, sl.stream, sl.h_totals, sl.cap);
+  if(rc == VGPU_OK)
+    rc = vgpu_list_phase_a(sl.q, sl.list);
+  if(rc == VGPU_OK && cudaLaunchHostFunc(sl.stream, on_stage_end, &sl) != cudaSuccess)
+    rc = VGPU_ERROR_DEVICE_LOST;
+  if(rc)
+  {
+    fail_batch(S, sl, rc);
+    return;
+  }
+  sl.stage = 1;
+}
+
+void scheduler(vgpu_server *S)
+{
+  cudaSetDevice(S->device);
+  for(;;)
+  {
+    std::vector<Slot *> ready;
+    bool stopping;
+    {
+      std::unique_lock<std::mutex> lk(S->ev_mu);
+      S->ev_cv.wait_for(lk, std::chrono::milliseconds(20), [&] { return S->wake || S->stop; });
+      S->wake = false;
+      stopping = S->stop;
+      for(Slot &sl : S->slots)
+        if(sl.signalled)
+        {
+          sl.signalled = false;
+          ready.push_back(&sl);
+        }
+    }
+    for(Slot *sl : ready)
+    {
+      if(sl->stage == 1)
+        start_raster(S, *sl);
+      else if(sl->stage == 2)
+        finish_batch(S, *sl);
+    }
+    if(stopping)
+    {
+      bool busy = false;
+      for(Slot &sl : S->slots)
+        busy |= sl.stage != 0;
+      if(!busy)
+      {
+        std::lock_guard<std::mutex> g(S->mu);
+        std::vector<Req *> rest(S->pending.begin(), S->pending.end());
+        S->pending.clear();
+        complete_locked(S, rest, VGPU_ERROR_INITIALIZATION_FAILED, vgpu_now_ns(), false);
+        return;
+      }
+      continue;
+    }
+    for(Slot &sl : S->slots)
+      if(sl.stage == 0)
+        launch_batch(S, sl);
+  }
+}
+
+void destroy_parts(vgpu_server *S)
+{
+  for(Slot &sl : S->slots)
+  {
+    if(sl.stream)
+      cudaStreamSynchronize(sl.stream);
+    vgpu_queue_destroy(sl.q);
+    if(sl.h_totals)
+      cudaFreeHost(sl.h_totals);
+  }
+  if(S->pool)
+    cudaMemPoolDestroy(S->pool);
+  for(Req *r : S->pending)
+    delete r;
+  delete S;
+}
+}    // namespace
+
+extern "C" int vgpu_server_create(const vgpu_server_config *cfg, vgpu_server **out)
+{
+  *out = nullptr;
+  int rc = vgpu_init();
+  if(rc)
+    return rc;
+  vgpu_server *S = new vgpu_server();
+  memset(&S->stats, 0, sizeof(S->stats));
+  S->cfg = *cfg;
+  if(!S->cfg.slots)
+    S->cfg.slots = kDefaultSlots;
+  if(!S->cfg.max_batch)
+    S->cfg.max_batch = kDefaultMaxBatch;
+  if(!S->cfg.max_batch_tris)
+    S->cfg.max_batch_tris = kDefaultMaxBatchTris;
+  if(!S->cfg.binning_pairs)
+    S->cfg.binning_pairs = kDefaultBinningPairs;
+  S->device = vgpu_device_ordinal();
+  if(cudaSetDevice(S->device) != cudaSuccess)
+  {
+    delete S;
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  }
+  cudaMemPoolProps props;
+  memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = S->device;
+  if(cudaMemPoolCreate(&S->pool, &props) != cudaSuccess)
+  {
+    cudaGetLastError();
+    S->pool = nullptr;
+    destroy_parts(S);
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  }
+  uint64_t keep = ~0ull; /* keep freed blocks for reuse instead of returning them */
+  cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  S->slots.resize(S->cfg.slots);
+  for(Slot &sl : S->slots)
+  {
+    sl.srv = S;
+    rc = vgpu_queue_create(&sl.q);
+    if(!rc)
+      rc = vgpu_queue_reserve_binning(sl.q, S->cfg.binning_pairs, 1u << 16);
+    if(rc)
+    {
+      destroy_parts(S);
+      return rc;
+    }
+    sl.stream = (cudaStream_t)vgpu_queue_stream(sl.q);
+    sl.cap = S->cfg.max_batch;
+    if(cudaMallocHost(&sl.h_totals, sl.cap * sizeof(uint32_t)) != cudaSuccess)
+    {
+      cudaGetLastError();
+      sl.h_totals = nullptr;
+      destroy_parts(S);
+      return VGPU_ERROR_OUT_OF_HOST_MEMORY;
+    }
+    S->binning += vgpu_queue_binning_bytes(sl.q);
+  }
+  S->stats.binning_bytes = S->binning;
+  if(S->binning >= S->cfg.budget_bytes)
+  {
+    fprintf(stderr, "visor_gb300: serving budget %llu bytes does not cover the slots' binning storage (%llu)\n",
+            (unsigned long long)S->cfg.budget_bytes, (unsigned long long)S->binning);
+    destroy_parts(S);
+    return VGPU_ERROR_OUT_OF_DEVICE_MEMORY;
+  }
+  S->th = std::thread(scheduler, S);
+  *out = S;
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_server_submit(vgpu_server *S, const vgpu_request *r, uint64_t *ticket)
+{
+  if(!r->program || !r->width || !r->height || r->width > kMaxTargetEdge || r->height > kMaxTargetEdge)
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  Req *q = new Req();
+  q->r = *r;
+  if(!q->r.arrival_ns)
+    q->r.arrival_ns = vgpu_now_ns();
+  q->tris = r->draw.num_tris;
+  const uint64_t px = (uint64_t)r->width * r->height;
+  const uint64_t rec = vgpu_program_record_words(r->program);
+  /* target, triangle records, tile counts and their scan levels, descriptors */
+  q->need = align256(px * 4) + align256(px * 4) + align256(q->tris * rec * 4) +
+            align256((q->tris + 1) * 4 + (q->tris / 1024 + 64) * 4) + 4096;
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    q->ticket = S->next_ticket++;
+    S->pending.push_back(q);
+    S->stats.submitted++;
+  }
+  if(ticket)
+    *ticket = q->ticket;
+  wake(S);
+  return VGPU_OK;
+}
+
+extern "C" uint32_t vgpu_server_poll(vgpu_server *S, vgpu_completion *out, uint32_t max)
+{
+  std::lock_guard<std::mutex> g(S->mu);
+  uint32_t n = 0;
+  while(n < max && !S->done.empty())
+  {
+    out[n++] = S->done.front();
+    S->done.pop_front();
+  }
+  return n;
+}
+
+extern "C" int vgpu_server_wait(vgpu_server *S, uint64_t timeout_ns)
+{
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto idle = [&] { return S->pending.empty() && S->in_flight == 0; };
+  if(timeout_ns == ~0ull)
+  {
+    S->idle_cv.wait(lk, idle);
+    return VGPU_OK;
+  }
+  return S->idle_cv.wait_for(lk, std::chrono::nanoseconds(timeout_ns), idle) ? VGPU_OK : VGPU_TIMEOUT;
+}
+
+extern "C" int vgpu_server_stats_get(vgpu_server *S, vgpu_server_stats *out)
+{
+  std::lock_guard<std::mutex> g(S->mu);
+  *out = S->stats;
+  out->reserved_bytes = S->reserved;
+  out->in_flight = (uint32_t)S->in_flight;
+  return VGPU_OK;
+}
+
+extern "C" void vgpu_server_destroy(vgpu_server *S)
+{
+  if(!S)
+    return;
+  {
+    std::lock_guard<std::mutex> g(S->ev_mu);
+    S->stop = true;
+  }
+  S->ev_cv.notify_one();
+  if(S->th.joinable())
+    S->th.join();
+  destroy_parts(S);
+}

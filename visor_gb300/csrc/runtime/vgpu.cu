@@ -37,6 +37,7 @@
 
 #include "visor_gpu.h"
 #include "vgpu_noalloc.h"
+#include "vgpu_internal.h"
 #include "../kernels/vgx_tiles.cuh"
 
 #include "vgx_sources.inc" /* generated: kVgxTypes, kVgxDevice, kVgxTiles, kVgxStage */
@@ -476,6 +477,7 @@ struct VgpuVariant
 struct vgpu_program
 {
   std::string source; /* translated shaders */
+  u64 hash = 0;       /* of source: programs with equal sources share jobs */
   u32 k = 0, rec_words = 0;
   std::map<u32, VgpuVariant *> variants; /* key: tile_shift << 8 | warps */
   std::mutex mu;
@@ -639,6 +641,7 @@ extern "C" int vgpu_program_create(const char *shader_source, uint32_t tile_shif
     return VGPU_ERROR_INITIALIZATION_FAILED;
   vgpu_program *p = new vgpu_program();
   p->source = shader_source;
+  p->hash = hash_str(p->source);
   p->k = (u32)atoi(kd + 14);
   p->rec_words = ((20 + 3 * p->k) + 3) & ~3u;
   /* compile the default variant now, as vkCreateGraphicsPipelines compiles */
@@ -727,21 +730,47 @@ struct vgpu_list
   u32 *h_totals = nullptr; /* pinned: pair totals per job */
   u32 *d_totals = nullptr;
   u64 tris_in = 0;
+  /* stream-ordered storage (serving batches): device buffers come from `pool`
+     on `pool_stream` and h_totals belongs to the caller */
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t pool_stream = nullptr;
+  u32 *ext_totals = nullptr;
+  size_t ext_totals_cap = 0;
 };
 
 extern "C" vgpu_list *vgpu_list_create(void) { return new vgpu_list(); }
+
+static void list_dev_free(vgpu_list *l, void *p)
+{
+  if(!p)
+    return;
+  if(l->pool)
+    cudaFreeAsync(p, l->pool_stream);
+  else
+    cudaFree(p);
+}
+
+static int list_dev_alloc(vgpu_list *l, void **p, size_t bytes)
+{
+  if(l->pool)
+    CK(cudaMallocFromPoolAsync(p, bytes, l->pool, l->pool_stream));
+  else
+    CK(cudaMalloc(p, bytes));
+  return VGPU_OK;
+}
 
 static void list_free_device(vgpu_list *l)
 {
   for(Job &j : l->jobs)
   {
-    cudaFree(j.d_draws);
-    cudaFree(j.d_targets);
+    list_dev_free(l, j.d_draws);
+    list_dev_free(l, j.d_targets);
   }
-  cudaFree(l->d_records);
-  cudaFree(l->d_counts);
-  cudaFree(l->d_totals);
-  cudaFreeHost(l->h_totals);
+  list_dev_free(l, l->d_records);
+  list_dev_free(l, l->d_counts);
+  list_dev_free(l, l->d_totals);
+  if(!l->ext_totals)
+    cudaFreeHost(l->h_totals);
   l->d_records = l->d_counts = l->d_totals = l->h_totals = nullptr;
   l->jobs.clear();
   l->plan.clear();
@@ -884,7 +913,9 @@ static int list_build(vgpu_list *l)
     /* draw */
     u32 ntris = c.draw.num_tris;
     l->tris_in += ntris;
-    if(!open || !batched || open->prog != c.prog)
+    const bool same_code = open && (open->prog == c.prog || (open->prog->hash == c.prog->hash &&
+                                                              open->prog->source == c.prog->source));
+    if(!open || !batched || !same_code)
     {
       int vrc = VGPU_OK;
       VgpuVariant *var = get_variant(c.prog, g_tuning.bin_shift, g_tuning.raster_warps, &vrc);
@@ -964,18 +995,47 @@ static int list_build(vgpu_list *l)
       j.scan_levels.push_back(cnt_words);
       cnt_words += n + 1;
     }
-    CK(cudaMalloc(&j.d_draws, std::max<size_t>(1, j.draws.size()) * sizeof(VgxDraw)));
-    CK(cudaMalloc(&j.d_targets, std::max<size_t>(1, j.targets.size()) * sizeof(VgxTarget)));
-    CK(cudaMemcpy(j.d_draws, j.draws.data(), j.draws.size() * sizeof(VgxDraw), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(j.d_targets, j.targets.data(), j.targets.size() * sizeof(VgxTarget),
-                  cudaMemcpyHostToDevice));
+    int rc = list_dev_alloc(l, (void **)&j.d_draws,
+                            std::max<size_t>(1, j.draws.size()) * sizeof(VgxDraw));
+    if(!rc)
+      rc = list_dev_alloc(l, (void **)&j.d_targets,
+                          std::max<size_t>(1, j.targets.size()) * sizeof(VgxTarget));
+    if(rc)
+      return rc;
+    if(l->pool)
+    {
+      CK(cudaMemcpyAsync(j.d_draws, j.draws.data(), j.draws.size() * sizeof(VgxDraw),
+                         cudaMemcpyHostToDevice, l->pool_stream));
+      CK(cudaMemcpyAsync(j.d_targets, j.targets.data(), j.targets.size() * sizeof(VgxTarget),
+                         cudaMemcpyHostToDevice, l->pool_stream));
+    }
+    else
+    {
+      CK(cudaMemcpy(j.d_draws, j.draws.data(), j.draws.size() * sizeof(VgxDraw),
+                    cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(j.d_targets, j.targets.data(), j.targets.size() * sizeof(VgxTarget),
+                    cudaMemcpyHostToDevice));
+    }
   }
   l->records_words = rec_words;
   l->counts_words = cnt_words;
-  CK(cudaMalloc(&l->d_records, std::max<u64>(4, rec_words) * 4));
-  CK(cudaMalloc(&l->d_counts, std::max<u64>(4, cnt_words) * 4));
-  CK(cudaMalloc(&l->d_totals, std::max<size_t>(1, l->jobs.size()) * 4));
-  CK(cudaMallocHost(&l->h_totals, std::max<size_t>(1, l->jobs.size()) * 4));
+  int rc = list_dev_alloc(l, (void **)&l->d_records, std::max<u64>(4, rec_words) * 4);
+  if(!rc)
+    rc = list_dev_alloc(l, (void **)&l->d_counts, std::max<u64>(4, cnt_words) * 4);
+  if(!rc)
+    rc = list_dev_alloc(l, (void **)&l->d_totals, std::max<size_t>(1, l->jobs.size()) * 4);
+  if(rc)
+    return rc;
+  if(l->ext_totals)
+  {
+    if(l->jobs.size() > l->ext_totals_cap)
+      return VGPU_ERROR_OUT_OF_HOST_MEMORY;
+    l->h_totals = l->ext_totals;
+  }
+  else
+  {
+    CK(cudaMallocHost(&l->h_totals, std::max<size_t>(1, l->jobs.size()) * 4));
+  }
   l->built = true;
   return VGPU_OK;
 }
@@ -1716,3 +1776,100 @@ extern "C" int vgpu_submit_noalloc(vgpu_queue *q, vgpu_list *l)
   CK(cudaGetLastError());
   return VGPU_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* split submission for the serving engine (single-segment lists)            */
+/* ------------------------------------------------------------------------ */
+
+extern "C" int vgpu_list_build_pooled(vgpu_list *l, void *pool, void *stream, uint32_t *h_totals,
+                                      size_t h_totals_cap)
+{
+  l->pool = (cudaMemPool_t)pool;
+  l->pool_stream = (cudaStream_t)stream;
+  l->ext_totals = h_totals;
+  l->ext_totals_cap = h_totals_cap;
+  for(const Cmd &c : l->cmds)
+    if(c.type == CMD_COPY)
+      return VGPU_ERROR_INITIALIZATION_FAILED; /* copies would split the list into segments */
+  return list_build(l);
+}
+
+extern "C" void vgpu_list_destroy_pooled(vgpu_list *l)
+{
+  /* stream-ordered frees after everything already queued on the pool stream */
+  vgpu_list_destroy(l);
+}
+
+extern "C" int vgpu_list_phase_a(vgpu_queue *q, vgpu_list *l)
+{
+  if(!l->built)
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  q->rev_used = 0;
+  CK(cudaEventRecord(q->ev0, q->stream));
+  for(auto &u : l->uploads)
+    CK(cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, q->stream));
+  for(const Exec &x : l->plan)
+    if(x.kind == Exec::E_JOB)
+    {
+      int rc = run_setup(q, l, x.index);
+      if(rc)
+        return rc;
+    }
+  if(!l->jobs.empty())
+    CK(cudaMemcpyAsync(l->h_totals, l->d_totals, l->jobs.size() * 4, cudaMemcpyDeviceToHost,
+                       q->stream));
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_list_phase_b(vgpu_queue *q, vgpu_list *l)
+{
+  u32 mx = 0;
+  for(size_t i = 0; i < l->jobs.size(); i++)
+    mx = std::max(mx, l->h_totals[i]);
+  int rc = ensure_pairs(q, mx);
+  if(rc)
+    return rc;
+  for(const Exec &x : l->plan)
+  {
+    if(x.kind == Exec::E_CLEAR)
+    {
+      u64 n = (u64)x.target.width * x.target.height;
+      unsigned g = (unsigned)std::min<u64>((n + 255) / 256, (u64)g_sms * 16);
+      k_clear<<<std::max(g, 1u), 256, 0, q->stream>>>(x.target, x.color, x.depth);
+      q->launches++;
+    }
+    else if(x.kind == Exec::E_JOB)
+    {
+      rc = run_raster(q, l, x.index);
+      if(rc)
+        return rc;
+    }
+  }
+  for(auto &d : l->downloads)
+    CK(cudaMemcpyAsync(d.first, d.second.first, d.second.second, cudaMemcpyDeviceToHost, q->stream));
+  CK(cudaEventRecord(q->ev1, q->stream));
+  q->timed = true;
+  q->stats.tris_in += l->tris_in;
+  for(const Cmd &c : l->cmds)
+    if(c.type == CMD_DRAW)
+      q->stats.draws++;
+  q->stats.jobs += l->jobs.size();
+  CK(cudaGetLastError());
+  return VGPU_OK;
+}
+
+extern "C" uint64_t vgpu_queue_binning_bytes(const vgpu_queue *q)
+{
+  return (u64)q->pair_capacity * 16 + q->hist_words * 4 + (u64)q->tile_capacity * 12 +
+         q->scratch_words * 4;
+}
+
+extern "C" int vgpu_queue_reserve_binning(vgpu_queue *q, uint64_t pairs, uint32_t tiles)
+{
+  int rc = ensure_pairs(q, (u32)std::min<uint64_t>(pairs, 0xffffffffull));
+  if(!rc)
+    rc = ensure_tiles(q, tiles);
+  return rc;
+}
+
+extern "C" int vgpu_device_ordinal(void) { return g_device; }

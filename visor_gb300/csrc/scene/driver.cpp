@@ -17,6 +17,9 @@
 #include <vector>
 
 #include "visor_driver.h"
+#ifndef VISOR_DRIVER_KHRONOS_HEADER
+#include "visor_icd.h"
+#endif
 #include "visor_spirv.h"
 
 namespace
@@ -785,3 +788,43 @@ extern "C" void vsd_release(vsd_scene *s)
 extern "C" void *vsd_queue(vsd_context *c) { return (void *)c->queue; }
 
 extern "C" void *vsd_command_buffer(vsd_scene *s) { return (void *)s->cmd; }
+
+extern "C" int vsd_request(vsd_scene *s, uint32_t draw, void *out)
+{
+#ifdef VISOR_DRIVER_KHRONOS_HEADER
+  (void)s, (void)draw, (void)out;
+  return -1; /* the reference ICD has no serving entry points */
+#else
+  const vsc_scene *sc = s->scene;
+  if(draw >= sc->num_draws)
+    return -1;
+  const vsc_draw &d = sc->draws[draw];
+  const vsc_pass *pass = nullptr;
+  for(uint32_t i = 0; i < sc->num_passes; i++)
+    if(draw >= sc->passes[i].first_draw && draw < sc->passes[i].first_draw + sc->passes[i].draw_count)
+      pass = &sc->passes[i];
+  if(!pass)
+    return -1;
+  visor_gb300_request *r = (visor_gb300_request *)out;
+  memset(r, 0, sizeof(*r));
+  r->pipeline = s->pipelines[d.pipeline];
+  r->set = d.texture != VSC_NONE ? s->sets[d.texture * 3 + sc->pipelines[d.pipeline].filter]
+                                 : VK_NULL_HANDLE;
+  r->vertex_buffer = s->vb;
+  r->vertex_offset = d.vb_offset;
+  if(d.indexed)
+  {
+    r->index_buffer = s->ib;
+    r->index_type = VK_INDEX_TYPE_UINT32;
+  }
+  r->count = d.count;
+  r->first = d.first;
+  r->push_size = d.push_size;
+  memcpy(r->push, d.push, sizeof(r->push));
+  r->width = sc->targets[pass->target].width;
+  r->height = sc->targets[pass->target].height;
+  memcpy(r->clear_color, sc->clear_color, sizeof(r->clear_color));
+  r->clear_depth = sc->clear_depth;
+  return 0;
+#endif
+}

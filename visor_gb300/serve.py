@@ -1,0 +1,162 @@
+"""Serving: continuous batching of render requests over resident resources.
+
+A thin ctypes layer over the serving entry points of libvisor_gb300.so
+(`visor_gb300_server_create/submit` in include/visor_icd.h and the
+`vgpu_server_*` calls in include/visor_gpu.h).  A request is one draw of a
+scene that `Device.upload` made resident (pipeline, descriptor set, vertex and
+index buffers stay on the device), rendered into a new target of the scene's
+size.  The scheduler inside the library admits requests in arrival order under
+a device-memory budget and runs every admitted request of a free slot as one
+batched launch chain; several slots overlap on the device.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib as _lib
+
+VP = C.c_void_p
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("slots", C.c_uint32), ("max_batch", C.c_uint32),
+                ("max_batch_tris", C.c_uint64), ("binning_pairs", C.c_uint64)]
+
+
+class Request(C.Structure):
+    """visor_gb300_request (include/visor_icd.h)."""
+    _fields_ = [("pipeline", VP), ("set", VP), ("vertex_buffer", VP), ("vertex_offset", C.c_uint64),
+                ("index_buffer", VP), ("index_offset", C.c_uint64), ("index_type", C.c_int32),
+                ("count", C.c_uint32), ("first", C.c_uint32), ("push_size", C.c_uint32),
+                ("push", C.c_uint8 * 128), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("clear_color", C.c_float * 4), ("clear_depth", C.c_float),
+                ("out_color", VP), ("out_depth", VP), ("tag", C.c_uint64), ("arrival_ns", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32),
+                ("batch_size", C.c_uint32), ("arrival_ns", C.c_uint64), ("admit_ns", C.c_uint64),
+                ("done_ns", C.c_uint64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("batches", C.c_uint64), ("reserved_bytes", C.c_uint64),
+                ("peak_reserved_bytes", C.c_uint64), ("binning_bytes", C.c_uint64),
+                ("max_batch_seen", C.c_uint32), ("in_flight", C.c_uint32),
+                ("tris", C.c_uint64), ("shaded", C.c_uint64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+def bind(L):
+    if getattr(L, "_serve_bound", False):
+        return L
+    L.visor_gb300_server_create.argtypes = [VP, C.POINTER(ServerConfig), C.POINTER(VP)]
+    L.visor_gb300_server_create.restype = C.c_int
+    L.visor_gb300_server_submit.argtypes = [VP, C.POINTER(Request), C.POINTER(C.c_uint64)]
+    L.visor_gb300_server_submit.restype = C.c_int
+    L.vgpu_server_poll.argtypes = [VP, C.POINTER(Completion), C.c_uint32]
+    L.vgpu_server_poll.restype = C.c_uint32
+    L.vgpu_server_wait.argtypes = [VP, C.c_uint64]
+    L.vgpu_server_wait.restype = C.c_int
+    L.vgpu_server_stats_get.argtypes = [VP, C.POINTER(ServerStats)]
+    L.vgpu_server_stats_get.restype = C.c_int
+    L.vgpu_server_destroy.argtypes = [VP]
+    L.vgpu_server_destroy.restype = None
+    L.vgpu_now_ns.argtypes = []
+    L.vgpu_now_ns.restype = C.c_uint64
+    L.vgpu_host_alloc.argtypes = [C.c_uint64, C.POINTER(VP)]
+    L.vgpu_host_alloc.restype = C.c_int
+    L.vgpu_host_free.argtypes = [VP]
+    L.vgpu_host_free.restype = None
+    L.vsd_request.argtypes = [VP, C.c_uint32, C.POINTER(Request)]
+    L.vsd_request.restype = C.c_int
+    L._serve_bound = True
+    return L
+
+
+def now_ns():
+    return int(bind(_lib()).vgpu_now_ns())
+
+
+class PinnedBuffer:
+    """Page-locked host memory viewed as a numpy array."""
+
+    def __init__(self, nbytes):
+        L = bind(_lib())
+        self._lib = L
+        p = VP()
+        rc = L.vgpu_host_alloc(nbytes, C.byref(p))
+        if rc != 0:
+            raise MemoryError(f"pinned host allocation of {nbytes} bytes failed ({rc})")
+        self.ptr = p.value
+        self.nbytes = nbytes
+
+    def view(self, dtype, count, offset=0):
+        buf = (C.c_uint8 * (count * np.dtype(dtype).itemsize)).from_address(self.ptr + offset)
+        return np.frombuffer(buf, dtype=dtype, count=count)
+
+    def free(self):
+        if self.ptr:
+            self._lib.vgpu_host_free(self.ptr)
+            self.ptr = None
+
+
+def request_for(uploaded, draw=0):
+    """The serving request that renders `draw` of an uploaded scene."""
+    r = Request()
+    L = bind(uploaded.dev.lib)
+    if L.vsd_request(uploaded.sc, draw, C.byref(r)) != 0:
+        raise ValueError(f"scene has no draw {draw}")
+    return r
+
+
+class Server:
+    def __init__(self, device, budget_bytes, slots=0, max_batch=0, max_batch_tris=0,
+                 binning_pairs=0):
+        L = bind(device.lib)
+        self.lib = L
+        cfg = ServerConfig(budget_bytes=int(budget_bytes), slots=slots, max_batch=max_batch,
+                           max_batch_tris=max_batch_tris, binning_pairs=binning_pairs)
+        h = VP()
+        dev_handle = None
+        rc = L.visor_gb300_server_create(dev_handle, C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"server creation failed (VkResult {rc})")
+        self.h = h
+
+    def submit(self, request, out_color=None, out_depth=None, tag=0, arrival_ns=0):
+        """Enqueue; out_color / out_depth are host addresses (ints) or None."""
+        request.out_color = out_color
+        request.out_depth = out_depth
+        request.tag = tag
+        request.arrival_ns = arrival_ns
+        t = C.c_uint64()
+        rc = self.lib.visor_gb300_server_submit(self.h, C.byref(request), C.byref(t))
+        if rc != 0:
+            raise RuntimeError(f"submit failed (VkResult {rc})")
+        return t.value
+
+    def poll(self, max_items=256):
+        arr = (Completion * max_items)()
+        n = self.lib.vgpu_server_poll(self.h, arr, max_items)
+        return [arr[i].as_dict() for i in range(n)]
+
+    def wait(self, timeout_s=None):
+        ns = 2 ** 64 - 1 if timeout_s is None else int(timeout_s * 1e9)
+        return self.lib.vgpu_server_wait(self.h, ns) == 0
+
+    def stats(self):
+        s = ServerStats()
+        self.lib.vgpu_server_stats_get(self.h, C.byref(s))
+        return s.as_dict()
+
+    def close(self):
+        if self.h:
+            self.lib.vgpu_server_destroy(self.h)
+            self.h = None
