@@ -80,7 +80,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.reader = threading.Thread(target=self._read, daemon=True)
             self.reader.start()
@@ -209,8 +209,12 @@ def run_ours(args):
     dist, rank, world = _dist()
     vg.set_tuning(time_raster=1)
     dev = vg.Device()
-    params = {"count": args.triangles} if args.triangles else {}
-    h = vs.generate(vg.lib(), vs.CFG_TRIS, SEED, **params)
+    if args.frames:
+        # profiling aid: the timed loop on configuration 1 with `frames` sphere frames
+        h = vs.generate(vg.lib(), vs.CFG_SPHERE, SEED, count=args.frames)
+    else:
+        params = {"count": args.triangles} if args.triangles else {}
+        h = vs.generate(vg.lib(), vs.CFG_TRIS, SEED, **params)
     w, hgt = h.targets()[0]
     tris = h.triangle_count()
 
@@ -314,6 +318,14 @@ def run_ours(args):
         "gpu_launches": b["launches"],
         "shaded_per_step": b["shaded"], "covered_per_step": b["covered"],
     }
+    if rank == 0 and world == 1 and not args.no_configs and not args.only_batched:
+        dev2 = vg.Device()
+        try:
+            line["configs"] = secondary_configs(dev2, max(3, min(args.steps, 5)), 3, peak)
+            line["serving"] = serving_sweep(dev2, [100, 500, 1000, 2000, 5000], 1.5, 48,
+                                            100 << 30, 3)
+        finally:
+            dev2.close()
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             line["cpu_baseline"] = cpu_baseline()
@@ -322,6 +334,187 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+STRIDE = {1: 32, 2: 20, 3: 36}  # vertex bytes per shader layout (scene.c vsc_vertex_attrs)
+
+
+def model_bytes(h, covered, shaded):
+    """Immediate-mode fragment-stream bytes of one frame: per draw indices, referenced
+    vertices and 64 B of constants; per cleared pass W*H*8; 4 B depth read per covered
+    fragment; per shaded fragment 4 B colour + 4 B depth write (+ 4 B colour read when
+    blending, weighted by the blending draws' triangle share); bound textures once."""
+    import numpy as np
+    s = h.s
+    ib = np.ctypeslib.as_array(s.ib, shape=(s.ib_count,)) if s.ib_count else None
+    total, blend_tris, all_tris, tex = 0, 0, 0, set()
+    for i in range(s.num_draws):
+        d = s.draws[i]
+        p = s.pipelines[d.pipeline]
+        stride = STRIDE.get(p.shader, 32)
+        if d.indexed:
+            idx = ib[d.first:d.first + d.count]
+            total += 4 * d.count + (int(idx.max()) - int(idx.min()) + 1) * stride
+        else:
+            total += d.count * stride
+        total += 64
+        all_tris += d.count // 3
+        if p.blend_enable:
+            blend_tris += d.count // 3
+        if d.texture != 0xFFFFFFFF:
+            tex.add(d.texture)
+    for i in range(s.num_passes):
+        ps = s.passes[i]
+        if ps.clear:
+            t = s.targets[ps.target]
+            total += t.width * t.height * 8
+    blend_share = blend_tris / all_tris if all_tris else 0.0
+    total += covered * 4 + int(shaded * (8 + 4 * blend_share))
+    total += sum(s.textures[t].bytes for t in tex)
+    return total
+
+
+def measure_config(dev, h, steps, warmup, modes=("batched", "per_draw")):
+    """Device time per submit of a whole scene in each execution mode (L2 flushed),
+    the batched mode at the bin tile and warp count the autotuner picks for it."""
+    import visor_gb300 as vg
+    from visor_gb300 import tune
+    out = {}
+    choice, tuned = tune.tune(dev, h, vg.DEVICE_TARGETS, reps=2)
+    out["tuning"] = {"bin_tile": 1 << choice[0], "warps_per_bin": choice[1],
+                     "ms": {f"{1 << k[0]}x{1 << k[0]}/{k[1]}w": round(v, 4) for k, v in tuned.items()}}
+    for name in modes:
+        vg.set_mode(vg.MODE_BATCHED if name == "batched" else vg.MODE_PER_DRAW)
+        up = dev.upload(h, vg.DEVICE_TARGETS)
+        for _ in range(warmup):
+            up.submit()
+        ms, raster = [], []
+        launches = 0
+        for _ in range(steps):
+            dev.flush_l2()
+            dev.reset_stats()
+            up.submit()
+            st = dev.stats()
+            ms.append(st["gpu_ms"])
+            raster.append(st["raster_ms"])
+            launches += st["kernel_launches"]
+        up.release()
+        out[name] = {"ms": sum(ms) / len(ms), "raster_ms": sum(raster) / len(raster),
+                     "shaded": st["shaded"], "covered": st["covered"], "tris": st["tris_in"],
+                     "draws": st["draws"], "launches_per_step": launches / steps}
+    vg.set_mode(vg.MODE_BATCHED)
+    return out
+
+
+def secondary_configs(dev, steps, warmup, peak):
+    """Configurations 1, 3 and 4: batched against per-draw launches, roofline of config 1."""
+    import visor_gb300 as vg
+    from visor_gb300 import scene as vs
+    L = vg.lib()
+    res = {}
+    specs = [
+        ("cfg1_sphere_x1024", vs.CFG_SPHERE, {"count": 1024},
+         "1024 independent 512x512 frames of the textured UV sphere (4,096 triangles each), one submit"),
+        ("cfg3_10k_draws", vs.CFG_DRAWS, {},
+         "2560x1440, 10,000 indexed draws (12-50,000 triangles each, ~58.5M total), 64 mipmapped 512^2 "
+         "textures sampled trilinearly, Lambert, depth LESS"),
+        ("cfg4_1024_targets", vs.CFG_TARGETS, {},
+         "1,024 targets of 128x128, 500-20,000 triangles each (~5.0M total), half blended"),
+    ]
+    for name, cfg, params, desc in specs:
+        h = vs.generate(L, cfg, SEED, **params)
+        m = measure_config(dev, h, steps, warmup)
+        b, pd = m["batched"], m["per_draw"]
+        mb = model_bytes(h, b["covered"], b["shaded"])
+        res[name] = {
+            "workload": desc, "tuning": m["tuning"],
+            "batched": {"shaded_gfrags_per_s": b["shaded"] / b["ms"] / 1e6,
+                        "mtris_per_s": b["tris"] / b["ms"] / 1e3, "ms_per_step": b["ms"],
+                        "raster_ms": b["raster_ms"], "launches_per_step": b["launches_per_step"]},
+            "per_draw": {"shaded_gfrags_per_s": pd["shaded"] / pd["ms"] / 1e6,
+                         "mtris_per_s": pd["tris"] / pd["ms"] / 1e3, "ms_per_step": pd["ms"],
+                         "launches_per_step": pd["launches_per_step"]},
+            "batched_over_per_draw": pd["ms"] / b["ms"],
+            "draws": b["draws"], "triangles": b["tris"], "shaded": b["shaded"], "covered": b["covered"],
+            "roofline_frame": {"model_bytes": mb, "achieved_gbs": mb / b["ms"] / 1e6, "peak_gbs": peak,
+                               "frac": mb / b["ms"] / 1e6 / peak},
+        }
+        del h
+    return res
+
+
+def serving_sweep(dev, rates, seconds, pool_size, budget, slots):
+    """Configuration 5: Poisson arrivals at each rate; frames/s and p50/p99 end-to-end latency
+    (scheduled arrival to result in host memory)."""
+    import numpy as np
+    import visor_gb300 as vg
+    from visor_gb300 import scene as vs
+    from visor_gb300 import serve
+    vg.set_mode(vg.MODE_BATCHED)
+    L = vg.lib()
+    pool = []
+    for i in range(pool_size):
+        h = vs.generate(L, vs.CFG_SERVING, SEED, count=i)
+        up = dev.upload(h, vg.DEVICE_TARGETS)
+        w, hh = h.targets()[0]
+        pool.append({"h": h, "up": up, "req": serve.request_for(up), "px": w * hh,
+                     "tris": h.triangle_count()})
+    ring_n = 192
+    ring = [serve.PinnedBuffer(1920 * 1080 * 4) for _ in range(ring_n)]
+    srv = serve.Server(dev, budget, slots=slots)
+    out = {"budget_bytes": budget, "slots": slots, "pool_requests": pool_size,
+           "pool_mean_tris": float(np.mean([p["tris"] for p in pool])),
+           "pool_mean_pixels": float(np.mean([p["px"] for p in pool])), "rates": []}
+    try:
+        for i, p in enumerate(pool):  # warm-up: every resident request once
+            srv.submit(p["req"], out_color=ring[i % ring_n].ptr, tag=i)
+            if i % ring_n == ring_n - 1:
+                srv.wait()
+        srv.wait()
+        srv.poll(4096)
+        rng = np.random.default_rng(SEED)
+        for rate in rates:
+            n = int(min(max(100, rate * seconds), 3000))
+            gaps = rng.exponential(1.0 / rate, size=n)
+            picks = rng.integers(0, pool_size, size=n)
+            free = list(range(ring_n))
+            owner = {}
+            done = []
+            st0 = srv.stats()
+            t0 = serve.now_ns() + 2_000_000
+            arrivals = t0 + (np.cumsum(gaps) * 1e9).astype(np.int64)
+            for k in range(n):
+                while True:
+                    for c in srv.poll(256):
+                        free.append(owner.pop(c["tag"]))
+                        done.append(c)
+                    if free and serve.now_ns() >= arrivals[k]:
+                        break
+                slot = free.pop()
+                owner[k] = slot
+                srv.submit(pool[picks[k]]["req"], out_color=ring[slot].ptr, tag=k,
+                           arrival_ns=int(arrivals[k]))
+            srv.wait()
+            done += srv.poll(4096)
+            st1 = srv.stats()
+            lat = np.array([(c["done_ns"] - c["arrival_ns"]) / 1e6 for c in done if c["status"] == 0])
+            batch = np.array([c["batch_size"] for c in done])
+            span = (max(c["done_ns"] for c in done) - t0) / 1e9
+            out["rates"].append({
+                "rate_per_s": rate, "requests": n, "completed": int(len(lat)),
+                "frames_per_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "mean_batch": float(batch.mean()), "batches": st1["batches"] - st0["batches"],
+                "shaded_gfrags_per_s": (st1["shaded"] - st0["shaded"]) / span / 1e9,
+                "mtris_per_s": (st1["tris"] - st0["tris"]) / span / 1e6,
+                "peak_reserved_gb": st1["peak_reserved_bytes"] / 1e9})
+    finally:
+        srv.close()
+        for b in ring:
+            b.free()
+        for p in pool:
+            p["up"].release()
+    return out
 
 
 class _Null:
@@ -341,8 +534,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--triangles", type=int, default=0,
                     help="smaller triangle count of the same workload (profiling captures)")
+    ap.add_argument("--frames", type=int, default=0,
+                    help="time configuration 1 with this many sphere frames instead (profiling captures)")
     ap.add_argument("--bin-shift", type=int, default=0, help="fix the bin tile (log2 edge) instead of autotuning")
     ap.add_argument("--warps", type=int, default=1, help="warps per bin when --bin-shift is given")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip configurations 1, 3, 4 and the serving sweep")
     ap.add_argument("--only-batched", action="store_true",
                     help="time only the batched device-resident path (profiling captures)")
     args = ap.parse_args()

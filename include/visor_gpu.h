@@ -116,7 +116,8 @@ void *vgpu_queue_stream(vgpu_queue *q);
 /* Overwrite a buffer larger than L2 on the queue's stream (benchmark hygiene). */
 int vgpu_queue_flush_l2(vgpu_queue *q);
 
-/* Tuning knobs read at list build time (autotuner, see tune.py). */
+/* Tuning knobs read at list build time (autotuner, see tune.py).  A list is built
+   again on its next vgpu_submit after bin_shift or raster_warps change. */
 typedef struct vgpu_tuning {
   uint32_t raster_blocks_per_sm; /* persistent raster CTAs per SM (0: 32 warps' worth) */
   uint32_t use_graphs;           /* replay batched lists as CUDA graphs */

@@ -380,13 +380,24 @@ __device__ __forceinline__ float vgx_plane_depth(const VgxPlane &p, int dx, int 
          n[2] * __uint_as_float(p.d.z);
 }
 
+/* Per-warp shared memory.  Planes are stored as separate arrays of uint4 so
+   that lanes reading different triangles' planes hit different banks. */
 struct VgxWarpShared
 {
-  VgxPlane plane[32];
+  uint4 pe[32], pa[32], pb[32], pd[32];
   float4 col[32];
-  u32 pass[32][2];
-  u32 off[32];
+  u32 frag[32]; /* fragment window: triangle | pixel-half << 5 | owner lane << 6 */
 };
+
+__device__ __forceinline__ VgxPlane vgx_plane_load(const VgxWarpShared &sh, u32 t)
+{
+  VgxPlane p;
+  p.e = sh.pe[t];
+  p.a = sh.pa[t];
+  p.b = sh.pb[t];
+  p.d = sh.pd[t];
+  return p;
+}
 
 /*
  * One warp, one 8x8 sub-tile at (x0, y0), one batch of n <= 32 triangles whose
@@ -402,7 +413,6 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
 {
   const VgxDraw *draws = (const VgxDraw *)job.draws;
   const int ldx = lane & 7, ldy = lane >> 3;
-  VgxPlane *pl = sh.plane;
 
   /* lane t: its triangle's planes at the sub-tile origin, coverage mask, depth bounds */
   u32 mlo = 0, mhi = 0, st = 0;
@@ -423,13 +433,11 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     const int e0 = a0 * x0 + b0 * y0 + bm * (r[R_AREA2] - c1 - c2);
     st = (u32)r[R_STATE];
     const int area = r[R_AREA2] < 0 ? -r[R_AREA2] : r[R_AREA2];
-    VgxPlane p;
-    p.e = make_uint4((u32)e0, (u32)e1, (u32)e2, st);
-    p.a = make_uint4((u32)a0, (u32)a1, (u32)a2, (u32)r[R_INVAREA]);
-    p.b = make_uint4((u32)b0, (u32)b1, (u32)b2, rec_index);
-    p.d = make_uint4((u32)r[R_DEPTH], (u32)r[R_DEPTH + 1], (u32)r[R_DEPTH + 2],
-                     area < (1 << 22) ? PF_SMALL : 0u);
-    pl[lane] = p;
+    sh.pe[lane] = make_uint4((u32)e0, (u32)e1, (u32)e2, st);
+    sh.pa[lane] = make_uint4((u32)a0, (u32)a1, (u32)a2, (u32)r[R_INVAREA]);
+    sh.pb[lane] = make_uint4((u32)b0, (u32)b1, (u32)b2, rec_index);
+    sh.pd[lane] = make_uint4((u32)r[R_DEPTH], (u32)r[R_DEPTH + 1], (u32)r[R_DEPTH + 2],
+                             area < (1 << 22) ? PF_SMALL : 0u);
     /* coverage of the sub-tile, clipped to the bbox [min, max) (rasterizer.cpp:538-549) */
     const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
     const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
@@ -527,7 +535,7 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     {
       const u32 t = __ffs(m) - 1;
       m &= m - 1;
-      const VgxPlane pt = pl[t];
+      const VgxPlane pt = vgx_plane_load(sh, t);
       const u32 stt = pt.e.w;
       float nn[3];
       const float z = vgx_plane_depth(pt, ldx, dy, nn);
@@ -542,10 +550,23 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
       }
     }
   }
+  shaded_total += __popc(pass[0]) + __popc(pass[1]);
+  /* Without blending a fragment replaces the pixel's colour bytes (the alpha byte is
+     never written, rasterizer.cpp:674-676) and shaders have no side effects, so only
+     a pixel's last passing opaque fragment of the batch and the ones after it can
+     reach memory: the earlier ones are counted but not shaded. */
+  const u32 opaque = __ballot_sync(0xffffffffu, (u32)lane < n && !(st & S_BLEND));
+#pragma unroll
+  for(int p = 0; p < 2; p++)
+  {
+    const u32 o = pass[p] & opaque;
+    if(o)
+      pass[p] &= ~((1u << (31 - __clz(o))) - 1u);
+  }
   const u32 mine = __popc(pass[0]) + __popc(pass[1]);
-  shaded_total += mine;
 
-  /* compact the passing fragments across the warp */
+  /* fragment order: lane by lane, each lane's first pixel then its second, triangles
+     ascending (any order works: a pixel's fragments stay in primitive order) */
   u32 incl = mine;
 #pragma unroll
   for(int o = 1; o < 32; o <<= 1)
@@ -556,36 +577,36 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
   }
   const u32 total = __shfl_sync(0xffffffffu, incl, 31);
   const u32 excl = incl - mine;
-  sh.off[lane] = excl;
-  sh.pass[lane][0] = pass[0];
-  sh.pass[lane][1] = pass[1];
-  __syncwarp();
+  u32 wm0 = pass[0], wm1 = pass[1]; /* fragments not yet placed in a window */
+  u32 bm0 = pass[0], bm1 = pass[1]; /* fragments not yet blended */
+  u32 wnext = excl, bnext = excl;
 
   for(u32 chunk = 0; chunk < total; chunk += 32)
   {
-    const u32 f = chunk + lane;
-    if(f < total)
+    /* place this lane's fragments that fall into the window [chunk, chunk + 32) */
+    while(wnext < excl + mine && wnext < chunk + 32)
     {
-      u32 olo = 0, ohi = 31;
-      while(olo < ohi)
+      u32 e;
+      if(wm0)
       {
-        u32 mid = (olo + ohi + 1) >> 1;
-        if(sh.off[mid] <= f)
-          olo = mid;
-        else
-          ohi = mid - 1;
+        e = (u32)(__ffs(wm0) - 1);
+        wm0 &= wm0 - 1;
       }
-      const u32 k = f - sh.off[olo];
-      const u32 p0 = sh.pass[olo][0];
-      const u32 c0 = __popc(p0);
-      const int sel = k < c0 ? 0 : 1;
-      u32 m = sel ? sh.pass[olo][1] : p0;
-      u32 kk = sel ? k - c0 : k;
-      while(kk--)
-        m &= m - 1;
-      const u32 t = __ffs(m) - 1;
-      const int fdx = (int)(olo & 7), fdy = (int)(olo >> 3) + 4 * sel;
-      const VgxPlane pt = pl[t];
+      else
+      {
+        e = (u32)(__ffs(wm1) - 1) | 32u;
+        wm1 &= wm1 - 1;
+      }
+      sh.frag[wnext - chunk] = e | ((u32)lane << 6);
+      wnext++;
+    }
+    __syncwarp();
+    if(chunk + lane < total)
+    {
+      const u32 e = sh.frag[lane];
+      const u32 t = e & 31u, sel = (e >> 5) & 1u, owner = e >> 6;
+      const int fdx = (int)(owner & 7), fdy = (int)(owner >> 3) + 4 * (int)sel;
+      const VgxPlane pt = vgx_plane_load(sh, t);
       const u32 *g = (const u32 *)job.records + (u64)pt.b.w * VGX_REC;
       float nb[4];
       (void)vgx_plane_depth(pt, fdx, fdy, nb);
@@ -606,24 +627,29 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
                             __uint_as_float(__ldg(g + R_LOD)));
     }
     __syncwarp();
-    /* in-order blend: each owner consumes its fragments of this chunk */
-    const u32 lo_f = max(excl, chunk), hi_f = min(excl + mine, chunk + 32);
-    for(u32 gg = lo_f; gg < hi_f; gg++)
+    /* in-order blend: each owner consumes its fragments of this window */
+    while(bnext < excl + mine && bnext < chunk + 32)
     {
-      const u32 k = gg - excl;
-      const u32 c0 = __popc(pass[0]);
-      const int sel = k < c0 ? 0 : 1;
-      u32 m = sel ? pass[1] : pass[0];
-      u32 kk = sel ? k - c0 : k;
-      while(kk--)
-        m &= m - 1;
-      const u32 t = __ffs(m) - 1;
-      const float4 c = sh.col[gg - chunk];
-      const u32 stt = pl[t].e.w;
+      u32 t, sel;
+      if(bm0)
+      {
+        t = (u32)(__ffs(bm0) - 1);
+        bm0 &= bm0 - 1;
+        sel = 0;
+      }
+      else
+      {
+        t = (u32)(__ffs(bm1) - 1);
+        bm1 &= bm1 - 1;
+        sel = 1;
+      }
+      const float4 c = sh.col[bnext - chunk];
+      const u32 stt = sh.pe[t].w;
       if(sel == 0)
         col[0] = vgx_blend_write(stt, c, col[0]);
       else
         col[1] = vgx_blend_write(stt, c, col[1]);
+      bnext++;
     }
     __syncwarp();
   }
@@ -651,32 +677,30 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
   const VgxTarget *targets = (const VgxTarget *)job.targets;
   const u32 *vals = (const u32 *)job.vals;
   const u32 *tstart = (const u32 *)job.tile_start, *tend = (const u32 *)job.tile_end;
-  const u32 nwork = job.all_tiles ? job.num_tiles : status[3];
+  const uint2 *work = (const uint2 *)job.work; /* (bin tile, target) of every bin with triangles */
+  const u32 nwork = status[3];
   u64 covered_total = 0, shaded_total = 0, tested_total = 0;
   const int ldx = lane & 7, ldy = lane >> 3;
   VgxWarpShared &sh = wsh[wib];
 
+  /* thread 0 claims the next bin while the CTA works on the current one */
+  u32 next = 0;
+  if(threadIdx.x == 0)
+    next = atomicAdd(&status[2], 1u);
   for(;;)
   {
     if(threadIdx.x == 0)
-      s_bin = atomicAdd(&status[2], 1u);
+      s_bin = next;
     __syncthreads();
     const u32 w = s_bin;
     __syncthreads();
     if(w >= nwork)
       break;
-    const u32 tile = job.work ? ((const u32 *)job.work)[w] : w;
-
-    u32 lo = 0, hi = job.num_targets - 1;
-    while(lo < hi)
-    {
-      u32 mid = (lo + hi + 1) >> 1;
-      if(targets[mid].tile_base <= tile)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const VgxTarget T = targets[lo];
+    if(threadIdx.x == 0)
+      next = atomicAdd(&status[2], 1u);
+    const uint2 wt = work[w];
+    const u32 tile = wt.x;
+    const VgxTarget T = targets[wt.y];
     const u32 local = tile - T.tile_base;
     const int bx0 = (int)(local % T.tiles_x) << VGX_TILE_SHIFT;
     const int by0 = (int)(local / T.tiles_x) << VGX_TILE_SHIFT;

@@ -117,6 +117,7 @@ bool g_init = false;
 int g_sms = 148;
 int g_device = 0;
 vgpu_tuning g_tuning = {0, 1, 0, 3, 1};
+u32 g_tuning_gen = 1; /* bumped when a knob that shapes lists (bin tile, warps) changes */
 
 /* ------------------------------------------------------------------------ */
 /* generic kernels                                                           */
@@ -316,10 +317,21 @@ __global__ void k_radix_scatter(const u32 *keys, const u32 *vals, u32 n, u32 shi
   }
 }
 
-/* per-tile [start, end) of the sorted pairs, and the queue of non-empty tiles */
+constexpr u32 kRangesSharedTargets = 2048;
+
+/* per-tile [start, end) of the sorted pairs, and the queue of non-empty tiles as
+   (tile, target) pairs; targets are ordered by tile_base */
 __global__ void k_ranges(const u32 *keys, const u32 *pair_total, u32 capacity, u32 *tstart,
-                         u32 *tend, u32 *work, u32 *status)
+                         u32 *tend, uint2 *work, u32 *status, const VgxTarget *targets,
+                         u32 num_targets)
 {
+  /* the targets' first tiles, staged in shared memory when they fit */
+  __shared__ u32 s_base[kRangesSharedTargets];
+  const bool staged = num_targets <= kRangesSharedTargets;
+  if(staged)
+    for(u32 t = threadIdx.x; t < num_targets; t += blockDim.x)
+      s_base[t] = targets[t].tile_base;
+  __syncthreads();
   const u32 n = *pair_total;
   if(n > capacity)
     return;
@@ -329,11 +341,60 @@ __global__ void k_ranges(const u32 *keys, const u32 *pair_total, u32 capacity, u
     if(i == 0 || keys[i - 1] != k)
     {
       tstart[k] = i;
-      if(work)
-        work[atomicAdd(&status[3], 1u)] = k;
+      u32 lo = 0, hi = num_targets - 1;
+      while(lo < hi)
+      {
+        const u32 mid = (lo + hi + 1) >> 1;
+        if((staged ? s_base[mid] : targets[mid].tile_base) <= k)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      work[atomicAdd(&status[3], 1u)] = make_uint2(k, lo);
     }
     if(i == n - 1 || keys[i + 1] != k)
       tend[k] = i + 1;
+  }
+}
+
+/* Clear values into the pixels of cleared targets whose bin tile has no
+   triangles (tend == 0); tiles with triangles are cleared inside the raster.
+   One grid row per target (strided), four pixels of a row per thread. */
+__global__ void k_clear_empty(const VgxTarget *targets, u32 num_targets, u32 shift, const u32 *tend)
+{
+  for(u32 ti = blockIdx.y; ti < num_targets; ti += gridDim.y)
+  {
+    const VgxTarget T = targets[ti];
+    if(!T.init_clear)
+      continue;
+    const u32 W = (u32)T.width, H = (u32)T.height;
+    const u32 qpr = (W + 3) >> 2;
+    const u32 nq = qpr * H;
+    u32 *color = (u32 *)T.color;
+    float *depth = (float *)T.depth;
+    for(u32 q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+    {
+      const u32 y = q / qpr, x = (q - y * qpr) << 2;
+      if(tend[T.tile_base + (y >> shift) * T.tiles_x + (x >> shift)])
+        continue;
+      const u64 pix = (u64)y * W + x;
+      if(x + 4 <= W && (pix & 3) == 0)
+      {
+        ((uint4 *)color)[pix >> 2] = make_uint4(T.clear_bgra, T.clear_bgra, T.clear_bgra, T.clear_bgra);
+        if(depth)
+          ((float4 *)depth)[pix >> 2] =
+              make_float4(T.clear_depth, T.clear_depth, T.clear_depth, T.clear_depth);
+      }
+      else
+      {
+        for(u32 i = 0; i < 4 && x + i < W; i++)
+        {
+          color[pix + i] = T.clear_bgra;
+          if(depth)
+            depth[pix + i] = T.clear_depth;
+        }
+      }
+    }
   }
 }
 
@@ -721,6 +782,7 @@ struct vgpu_list
   std::vector<std::pair<void *, std::pair<const void *, u64>>> uploads, downloads;
   int mode = VGPU_MODE_BATCHED;
   bool built = false;
+  u32 built_gen = 0; /* tuning generation the jobs were formed under */
   std::vector<Job> jobs;
   std::vector<Exec> plan;
   u32 *d_records = nullptr;
@@ -1037,6 +1099,7 @@ static int list_build(vgpu_list *l)
     CK(cudaMallocHost(&l->h_totals, std::max<size_t>(1, l->jobs.size()) * 4));
   }
   l->built = true;
+  l->built_gen = g_tuning_gen;
   return VGPU_OK;
 }
 
@@ -1154,7 +1217,7 @@ static int ensure_tiles(vgpu_queue *q, u32 tiles)
   cudaFree(q->work);
   CK(cudaMalloc(&q->tstart, (size_t)cap * 4));
   CK(cudaMalloc(&q->tend, (size_t)cap * 4));
-  CK(cudaMalloc(&q->work, (size_t)cap * 4));
+  CK(cudaMalloc(&q->work, (size_t)cap * 8)); /* (tile, target) per bin */
   q->tile_capacity = cap;
   return VGPU_OK;
 }
@@ -1204,7 +1267,7 @@ static VgxJob make_job(vgpu_queue *q, vgpu_list *l, Job &j, size_t ji)
   J.vals_alt = (u64)q->vals[1];
   J.tile_start = (u64)q->tstart;
   J.tile_end = (u64)q->tend;
-  J.work = j.all_tiles ? 0 : (u64)q->work;
+  J.work = (u64)q->work;
   J.status = (u64)q->status;
   J.counters = (u64)q->counters;
   J.scratch = (u64)q->scratch;
@@ -1226,6 +1289,21 @@ static int launch(vgpu_queue *q, CUfunction f, unsigned grid, unsigned block, Vg
   CU(g_cu.launchKernel(f, grid, 1, 1, block, 1, 1, 0, (CUstream)q->stream, args, nullptr));
   q->launches++;
   return VGPU_OK;
+}
+
+/* clears of the empty bin tiles of a job's cleared targets */
+static void launch_clear_empty(cudaStream_t stream, const Job &j, const u32 *tend)
+{
+  u32 max_quads = 1;
+  for(const VgxTarget &t : j.targets)
+    max_quads = std::max<u32>(max_quads, (((u32)t.width + 3) >> 2) * (u32)t.height);
+  const u32 nt = (u32)j.targets.size();
+  /* about 16 CTAs of 256 threads per SM in total */
+  u32 gx = (max_quads + 255) / 256;
+  const u32 want = std::max<u32>(1, (u32)g_sms * 16 / std::max<u32>(nt, 1));
+  gx = std::max<u32>(1, std::min(gx, want));
+  const u32 gy = std::min<u32>(nt, 65535);
+  k_clear_empty<<<dim3(gx, gy), 256, 0, stream>>>(j.d_targets, nt, j.var->tile_shift, tend);
 }
 
 /* phase A of a job: setup + scan of tile counts; total pairs -> d_totals[ji] */
@@ -1305,17 +1383,23 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
     CK(cudaMemcpyAsync(q->status + 1, counts + j.num_tris, 4, cudaMemcpyDeviceToDevice, q->stream));
     unsigned rg = std::min<u32>((total + 255) / 256, (u32)g_sms * 8);
     k_ranges<<<rg, 256, 0, q->stream>>>(q->keys[src], q->status + 1, q->pair_capacity, q->tstart,
-                                        q->tend, j.all_tiles ? nullptr : q->work, q->status);
+                                        q->tend, (uint2 *)q->work, q->status, j.d_targets,
+                                        (u32)j.targets.size());
     q->launches++;
   }
-  if(!j.all_tiles && !total)
+  if(j.all_tiles)
+  {
+    launch_clear_empty(q->stream, j, q->tend);
+    q->launches++;
+  }
+  if(!total)
     return VGPU_OK;
   /* persistent CTAs: enough to fill the SMs (32 warps each), never more than bins */
   const unsigned warps = j.var->warps;
   const unsigned per_sm = g_tuning.raster_blocks_per_sm ? g_tuning.raster_blocks_per_sm
                                                         : std::max(1u, 32u / warps);
   unsigned grid = std::max(1u, (unsigned)g_sms * per_sm);
-  const u32 bins = j.all_tiles ? j.num_tiles : total;
+  const u32 bins = std::min(j.num_tiles, total);
   grid = std::max(1u, std::min<unsigned>(grid, bins));
   if(g_tuning.time_raster)
   {
@@ -1338,7 +1422,7 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
 
 extern "C" int vgpu_submit(vgpu_queue *q, vgpu_list *l)
 {
-  if(!l->built)
+  if(!l->built || l->built_gen != g_tuning_gen)
   {
     int rc = list_build(l);
     if(rc)
@@ -1523,7 +1607,12 @@ extern "C" void vgpu_queue_reset_stats(vgpu_queue *q)
   q->launches = 0;
 }
 
-extern "C" void vgpu_set_tuning(const vgpu_tuning *t) { g_tuning = *t; }
+extern "C" void vgpu_set_tuning(const vgpu_tuning *t)
+{
+  if(t->bin_shift != g_tuning.bin_shift || t->raster_warps != g_tuning.raster_warps)
+    g_tuning_gen++;
+  g_tuning = *t;
+}
 extern "C" void vgpu_get_tuning(vgpu_tuning *t) { *t = g_tuning; }
 
 /* Overwrite a buffer larger than L2 on the queue's stream (benchmark hygiene). */
@@ -1553,7 +1642,7 @@ constexpr u32 kFixedTiles = 1u << 17; /* bin tiles per job */
 constexpr u64 kFixedHistWords = (u64)(kFixedPairs / kSortTile) * 256 + 256;
 constexpr u64 kFixedScanWords = 1024;
 constexpr u64 kFixedWords =
-    4ull * kFixedPairs + 3ull * kFixedTiles + kFixedHistWords + kFixedScanWords;
+    4ull * kFixedPairs + 4ull * kFixedTiles + kFixedHistWords + kFixedScanWords;
 constexpr int kFixedMaxDevices = 64;
 
 std::mutex g_fixed_mu;
@@ -1606,8 +1695,8 @@ static int fixed_buffers(FixedBufs *b)
   p += kFixedTiles;
   b->tend = p;
   p += kFixedTiles;
-  b->work = p;
-  p += kFixedTiles;
+  b->work = p; /* (tile, target) per bin */
+  p += 2ull * kFixedTiles;
   b->hist = p;
   p += kFixedHistWords;
   b->scan = p;
@@ -1625,7 +1714,7 @@ static int run_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, const FixedB
   J.vals_alt = (u64)b.vals[1];
   J.tile_start = (u64)b.tstart;
   J.tile_end = (u64)b.tend;
-  J.work = j.all_tiles ? 0 : (u64)b.work;
+  J.work = (u64)b.work;
   J.scratch = (u64)b.scan;
   J.pair_capacity = kFixedPairs;
   u32 *counts = l->d_counts + j.cnt_off;
@@ -1672,16 +1761,22 @@ static int run_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, const FixedB
     CK(cudaMemcpyAsync(q->status + 1, counts + j.num_tris, 4, cudaMemcpyDeviceToDevice, q->stream));
     unsigned rg = std::min<u32>((total + 255) / 256, (u32)g_sms * 8);
     k_ranges<<<rg, 256, 0, q->stream>>>(b.keys[src], q->status + 1, kFixedPairs, b.tstart, b.tend,
-                                        j.all_tiles ? nullptr : b.work, q->status);
+                                        (uint2 *)b.work, q->status, j.d_targets,
+                                        (u32)j.targets.size());
     q->launches++;
   }
-  if(!j.all_tiles && !total)
+  if(j.all_tiles)
+  {
+    launch_clear_empty(q->stream, j, b.tend);
+    q->launches++;
+  }
+  if(!total)
     return VGPU_OK;
   const unsigned warps = j.var->warps;
   const unsigned per_sm = g_tuning.raster_blocks_per_sm ? g_tuning.raster_blocks_per_sm
                                                         : std::max(1u, 32u / warps);
   unsigned grid = std::max(1u, (unsigned)g_sms * per_sm);
-  const u32 bins = j.all_tiles ? j.num_tiles : total;
+  const u32 bins = std::min(j.num_tiles, total);
   grid = std::max(1u, std::min<unsigned>(grid, bins));
   return launch(q, j.var->raster, grid, warps * 32, &J);
 }

@@ -4,6 +4,8 @@ Every candidate renders the same pixels (the configuration only changes how
 work is binned and distributed), so the tuner may time candidates on the real
 command buffer.  Each candidate lowers the command buffer again, replays it a
 few times and keeps the fastest device time (CUDA events around the submit).
+The scene is uploaded once: a command buffer's list is formed again on the
+first submit after the bin tile or warp count changes.
 """
 import visor_gb300 as vg
 
@@ -15,10 +17,10 @@ def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
     """Return (best (bin_shift, warps), {candidate: ms}) for a scene on a device."""
     results = {}
     vg.set_mode(mode)
-    for shift, warps in candidates or CANDIDATES:
-        vg.set_tuning(bin_shift=shift, raster_warps=warps)
-        up = dev.upload(handle, flags)
-        try:
+    up = dev.upload(handle, flags)
+    try:
+        for shift, warps in candidates or CANDIDATES:
+            vg.set_tuning(bin_shift=shift, raster_warps=warps)
             up.submit()
             best = None
             for _ in range(reps):
@@ -27,8 +29,8 @@ def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
                 ms = dev.stats()["gpu_ms"]
                 best = ms if best is None else min(best, ms)
             results[(shift, warps)] = best
-        finally:
-            up.release()
+    finally:
+        up.release()
     choice = min(results, key=results.get)
     vg.set_tuning(bin_shift=choice[0], raster_warps=choice[1])
     return choice, results
