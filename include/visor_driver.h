@@ -71,6 +71,10 @@ void *vsd_command_buffer(vsd_scene *s);
    Returns 0, or -1 when the draw does not exist. */
 int vsd_request(vsd_scene *s, uint32_t draw, void *request);
 
+/* Copy the scene's current vertex bytes (vsc_scene.vb) into its host-visible
+   staging buffer; with VSD_RESTAGE_INPUTS the next submit renders them. */
+int vsd_refresh_vertices(vsd_scene *s);
+
 /* Bytes copied host->device per submit when VSD_RESTAGE_INPUTS is set. */
 uint64_t vsd_restage_bytes(const vsd_scene *s);
 

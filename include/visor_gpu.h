@@ -108,6 +108,8 @@ typedef struct vgpu_stats {
   double raster_ms;    /* device time spent in raster kernels of the last submit */
   uint32_t status;     /* sticky device status bits */
   uint64_t depth_tested; /* covered fragments that reached the per-pixel depth test (not rejected per triangle) */
+  uint64_t graph_replays; /* submits replayed from a captured CUDA graph */
+  uint64_t graph_reruns;  /* replays whose geometry outgrew the graph's pair capacity, run again exactly */
 } vgpu_stats;
 int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out);
 void vgpu_queue_reset_stats(vgpu_queue *q);

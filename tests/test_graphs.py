@@ -1,0 +1,133 @@
+"""CUDA-graph replay of batched command lists.
+
+The first vkQueueSubmit of a command buffer runs with exact binning storage
+and records each job's pair total; the second captures the whole submission
+(uploads, setup, binning, raster, downloads) into a CUDA graph with those
+totals plus headroom as fixed capacities and launches it; later submits launch
+the same graph.
+Replays must give the oracle's frames bit for bit, and a replay whose geometry
+outgrew the capacity must be detected at the wait and rendered again exactly.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import visor_gb300 as vg
+from visor_gb300 import scene as vs
+from oracle import loader
+import scenes_edge
+
+pytestmark = pytest.mark.gpu
+
+SCENES = ["cfg2_small_blend", "cfg1_frames4", "cfg3_small_bilinear", "cfg4_small", "load_pass",
+          "blend_overlap", "depth_less", "strip", "texture_wrap"]
+
+
+@pytest.fixture(scope="module")
+def device():
+    d = vg.Device()
+    yield d
+    d.close()
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    return loader.Oracle()
+
+
+@pytest.fixture
+def graphs_on():
+    before = vg.get_tuning()
+    vg.set_mode(vg.MODE_BATCHED)
+    vg.set_tuning(use_graphs=1)
+    yield
+    vg.set_tuning(**before)
+
+
+def _equal(got, want):
+    (gc, gd), (wc, wd) = got, want
+    for a, b in zip(gc, wc):
+        if not np.array_equal(a, b):
+            return False
+    for a, b in zip(gd, wd):
+        if not np.array_equal(a.view(np.uint32), b.view(np.uint32)):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_replays_equal_oracle(device, oracle, graphs_on, name):
+    h = scenes_edge.build(device.lib, name)
+    cols, deps, counters = oracle.render(h)
+    up = device.upload(h)
+    try:
+        replays = 0
+        for i in range(4):
+            device.reset_stats()
+            up.submit()
+            st = device.stats()
+            replays += st["graph_replays"]
+            assert _equal(up.read(), (cols, deps)), f"submit {i}"
+            assert st["shaded"] == counters["shaded"] and st["covered"] == counters["covered"], i
+            assert st["graph_reruns"] == 0
+        assert replays == 3  # submit 2 captures and launches the graph, 3 and 4 launch it
+    finally:
+        up.release()
+
+
+def test_replay_that_outgrows_capacity_is_rendered_again(device, oracle, graphs_on):
+    """Vertices restaged every submit; after the graph is captured the triangles grow
+    16-fold in area, so the replay's pairs exceed its capacity."""
+    h = vs.generate(device.lib, vs.CFG_TRIS, 31, width=256, height=192, count=3000, max_area=30.0)
+    up = device.upload(h, vg.RESTAGE_INPUTS)
+    try:
+        for _ in range(3):
+            up.submit()
+        device.reset_stats()
+        up.submit()
+        assert device.stats()["graph_replays"] == 1
+        # clip-space positions are the first 16 bytes of each 20-byte vertex
+        nverts = h.s.vb_bytes // 20
+        raw = np.ctypeslib.as_array(h.s.vb, shape=(h.s.vb_bytes,))
+        pos = np.ndarray((nverts, 4), dtype=np.float32, buffer=raw, strides=(20, 4))
+        tri = pos[:, :2].reshape(-1, 3, 2)
+        centre = tri.mean(axis=1, keepdims=True)
+        tri[:] = centre + (tri - centre) * 4.0
+        up.refresh_vertices()
+        device.reset_stats()
+        up.submit()
+        st = device.stats()
+        assert st["graph_replays"] == 1 and st["graph_reruns"] == 1, st
+        cols, deps, counters = oracle.render(h)
+        assert _equal(up.read(), (cols, deps))
+        # the next submit captures a larger graph and replays it from then on
+        for _ in range(2):
+            device.reset_stats()
+            up.submit()
+            st = device.stats()
+            assert st["graph_reruns"] == 0
+            assert _equal(up.read(), (cols, deps))
+        assert st["graph_replays"] == 1
+    finally:
+        up.release()
+
+
+def test_graphs_off_gives_the_same_frames(device, oracle):
+    before = vg.get_tuning()
+    vg.set_mode(vg.MODE_BATCHED)
+    vg.set_tuning(use_graphs=0)
+    try:
+        h = scenes_edge.build(device.lib, "cfg2_small_blend")
+        cols, deps, _ = oracle.render(h)
+        up = device.upload(h)
+        try:
+            for _ in range(3):
+                device.reset_stats()
+                up.submit()
+                assert device.stats()["graph_replays"] == 0
+                assert _equal(up.read(), (cols, deps))
+        finally:
+            up.release()
+    finally:
+        vg.set_tuning(**before)

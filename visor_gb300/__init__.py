@@ -33,7 +33,8 @@ class VgpuStats(C.Structure):
                 ("covered", C.c_uint64), ("shaded", C.c_uint64), ("draws", C.c_uint64),
                 ("jobs", C.c_uint64), ("pairs", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("gpu_ms", C.c_double), ("raster_ms", C.c_double), ("status", C.c_uint32),
-                ("depth_tested", C.c_uint64)]
+                ("depth_tested", C.c_uint64), ("graph_replays", C.c_uint64),
+                ("graph_reruns", C.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -73,6 +74,8 @@ def lib():
     L.vsd_release.argtypes = [VP]
     L.vsd_queue.argtypes = [VP]
     L.vsd_queue.restype = VP
+    L.vsd_refresh_vertices.argtypes = [VP]
+    L.vsd_refresh_vertices.restype = C.c_int
     L.vsd_restage_bytes.argtypes = [VP]
     L.vsd_restage_bytes.restype = C.c_uint64
     L.vspv_emit.argtypes = [C.c_uint32, C.c_uint32, VP, C.c_size_t]
@@ -234,6 +237,12 @@ class UploadedScene:
             if rc != 0:
                 raise RuntimeError(f"reading target {i} failed ({rc})")
         return cols, deps
+
+    def refresh_vertices(self):
+        """Copy the scene's (possibly edited) vertex bytes into the staging buffer."""
+        rc = self.dev.lib.vsd_refresh_vertices(self.sc)
+        if rc != 0:
+            raise RuntimeError(f"vertex refresh failed ({rc})")
 
     def restage_bytes(self):
         return int(self.dev.lib.vsd_restage_bytes(self.sc))

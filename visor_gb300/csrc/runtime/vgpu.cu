@@ -255,8 +255,20 @@ constexpr int kSortBlock = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortBlock * kSortItems;
 
-__global__ void k_radix_hist(const u32 *keys, u32 n, u32 shift, u32 *hist, u32 nblocks)
+/* n_dev (optional): the real count on the device; n is then the capacity the grid
+   was sized for, and a count above it (overflow, flagged elsewhere) sorts nothing */
+__device__ __forceinline__ u32 radix_count(u32 n, const u32 *n_dev)
 {
+  if(!n_dev)
+    return n;
+  const u32 d = *n_dev;
+  return d <= n ? d : 0u;
+}
+
+__global__ void k_radix_hist(const u32 *keys, u32 n, const u32 *n_dev, u32 shift, u32 *hist,
+                             u32 nblocks)
+{
+  n = radix_count(n, n_dev);
   __shared__ u32 h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -271,9 +283,11 @@ __global__ void k_radix_hist(const u32 *keys, u32 n, u32 shift, u32 *hist, u32 n
   hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-__global__ void k_radix_scatter(const u32 *keys, const u32 *vals, u32 n, u32 shift,
-                                const u32 *hist_scanned, u32 nblocks, u32 *okeys, u32 *ovals)
+__global__ void k_radix_scatter(const u32 *keys, const u32 *vals, u32 n, const u32 *n_dev,
+                                u32 shift, const u32 *hist_scanned, u32 nblocks, u32 *okeys,
+                                u32 *ovals)
 {
+  n = radix_count(n, n_dev);
   __shared__ u32 base_d[256];
   __shared__ u32 wcnt[kSortBlock / 32][256];
   __shared__ u32 tot[256];
@@ -798,7 +812,17 @@ struct vgpu_list
   cudaStream_t pool_stream = nullptr;
   u32 *ext_totals = nullptr;
   size_t ext_totals_cap = 0;
+  /* CUDA-graph replay of batched lists */
+  bool have_totals = false;        /* h_totals hold the exact totals of a completed plain submit */
+  cudaGraphExec_t gexec = nullptr; /* the whole submit with fixed binning capacities */
+  vgpu_queue *gq = nullptr;        /* queue whose buffers the graph uses */
+  u32 g_buf_gen = 0;               /* that queue's buffer generation at capture */
+  u64 g_launches = 0, g_pairs = 0;
+  size_t g_rev = 0;                /* raster event pairs the graph records */
+  u32 *h_gstatus = nullptr;        /* pinned: status word as each replay left it */
 };
+
+static void graph_forget(vgpu_list *l);
 
 extern "C" vgpu_list *vgpu_list_create(void) { return new vgpu_list(); }
 
@@ -823,6 +847,8 @@ static int list_dev_alloc(vgpu_list *l, void **p, size_t bytes)
 
 static void list_free_device(vgpu_list *l)
 {
+  graph_forget(l);
+  l->have_totals = false;
   for(Job &j : l->jobs)
   {
     list_dev_free(l, j.d_draws);
@@ -844,6 +870,8 @@ extern "C" void vgpu_list_destroy(vgpu_list *l)
   if(!l)
     return;
   list_free_device(l);
+  if(l->h_gstatus)
+    cudaFreeHost(l->h_gstatus);
   delete l;
 }
 
@@ -1127,7 +1155,23 @@ struct vgpu_queue
   vgpu_stats stats;
   u64 launches = 0;
   bool timed = false;
+  u32 buf_gen = 1;                     /* bumped when a binning buffer is reallocated */
+  std::vector<vgpu_list *> gpending;   /* graph replays not yet checked for pair overflow */
+  std::recursive_mutex mu;             /* submissions and the checks at waits */
 };
+
+static void graph_forget(vgpu_list *l)
+{
+  if(l->gq)
+  {
+    auto &v = l->gq->gpending;
+    v.erase(std::remove(v.begin(), v.end(), l), v.end());
+  }
+  if(l->gexec)
+    cudaGraphExecDestroy(l->gexec);
+  l->gexec = nullptr;
+  l->gq = nullptr;
+}
 
 struct vgpu_fence
 {
@@ -1188,6 +1232,7 @@ static int ensure_pairs(vgpu_queue *q, u32 need)
   if(need <= q->pair_capacity)
     return VGPU_OK;
   u32 cap = std::max<u32>(need + need / 4, 1u << 20);
+  q->buf_gen++;
   for(int i = 0; i < 2; i++)
   {
     cudaFree(q->keys[i]);
@@ -1212,6 +1257,7 @@ static int ensure_tiles(vgpu_queue *q, u32 tiles)
   if(tiles <= q->tile_capacity)
     return VGPU_OK;
   u32 cap = std::max<u32>(tiles, 1u << 16);
+  q->buf_gen++;
   cudaFree(q->tstart);
   cudaFree(q->tend);
   cudaFree(q->work);
@@ -1226,6 +1272,7 @@ static int ensure_scratch(vgpu_queue *q, u64 words)
 {
   if(words <= q->scratch_words)
     return VGPU_OK;
+  q->buf_gen++;
   cudaFree(q->scratch);
   CK(cudaMalloc(&q->scratch, words * 4));
   q->scratch_words = words;
@@ -1353,7 +1400,7 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
     int src = 0;
     for(u32 shift = 0; shift < j.key_bits; shift += 8)
     {
-      k_radix_hist<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], total, shift, q->hist, nb);
+      k_radix_hist<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], total, nullptr, shift, q->hist, nb);
       std::vector<u64> lv;
       u64 n = (u64)nb * 256;
       u64 need = 0;
@@ -1372,8 +1419,8 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
       rc = scan_u32(q, q->hist, q->hist, n, q->scratch, lv, 0);
       if(rc)
         return rc;
-      k_radix_scatter<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], q->vals[src], total, shift,
-                                                        q->hist, nb, q->keys[src ^ 1],
+      k_radix_scatter<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], q->vals[src], total, nullptr,
+                                                        shift, q->hist, nb, q->keys[src ^ 1],
                                                         q->vals[src ^ 1]);
       q->launches += 2;
       src ^= 1;
@@ -1420,14 +1467,10 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
   return rc2;
 }
 
-extern "C" int vgpu_submit(vgpu_queue *q, vgpu_list *l)
+/* The submission with exact binning storage: per segment, setups, one host
+   synchronisation for the pair totals, then clears, binning and rasters. */
+static int submit_plain(vgpu_queue *q, vgpu_list *l)
 {
-  if(!l->built || l->built_gen != g_tuning_gen)
-  {
-    int rc = list_build(l);
-    if(rc)
-      return rc;
-  }
   q->rev_used = 0;
   CK(cudaEventRecord(q->ev0, q->stream));
   for(auto &u : l->uploads)
@@ -1503,6 +1546,278 @@ extern "C" int vgpu_submit(vgpu_queue *q, vgpu_list *l)
   return VGPU_OK;
 }
 
+/* ------------------------------------------------------------------------ */
+/* CUDA-graph replay                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* pair capacity a graph reserves for a job whose last exact total was `total` */
+static u32 graph_capacity(const Job &j, u32 total)
+{
+  if(!j.num_tris)
+    return 0;
+  const u64 c = (u64)total + total / 16 + 4096;
+  return (u32)std::min<u64>(c, 0xfffff000ull);
+}
+
+static void hist_levels(u32 cap, std::vector<u64> &lv, u64 &need)
+{
+  const u32 nb = (cap + kSortTile - 1) / kSortTile;
+  need = 0;
+  lv.clear();
+  for(u64 m = (u64)nb * 256; m > (u64)kScanTile;)
+  {
+    m = (m + kScanTile - 1) / kScanTile;
+    lv.push_back(need);
+    need += m + 1;
+  }
+}
+
+/* Phase B of a job with a fixed pair capacity and no host round trip: the
+   kernels read the real pair total on the device; a total above `cap` sets
+   VGX_STATUS_PAIR_OVERFLOW and the job rasterises nothing. */
+static int record_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, u32 cap)
+{
+  Job &j = l->jobs[ji];
+  VgxJob J = make_job(q, l, j, ji);
+  J.pair_capacity = cap;
+  u32 *counts = l->d_counts + j.cnt_off;
+  CK(cudaMemsetAsync(q->status + 1, 0, 12, q->stream));
+  CK(cudaMemsetAsync(q->tstart, 0, (size_t)j.num_tiles * 4, q->stream));
+  CK(cudaMemsetAsync(q->tend, 0, (size_t)j.num_tiles * 4, q->stream));
+  if(j.num_tris)
+  {
+    const u32 *total_dev = counts + j.num_tris;
+    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.prog->rec_words, counts);
+    q->launches++;
+    const u32 nb = (cap + kSortTile - 1) / kSortTile;
+    std::vector<u64> lv;
+    u64 need = 0;
+    hist_levels(cap, lv, need);
+    int src = 0;
+    for(u32 shift = 0; shift < j.key_bits; shift += 8)
+    {
+      k_radix_hist<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], cap, total_dev, shift, q->hist, nb);
+      int rc = scan_u32(q, q->hist, q->hist, (u64)nb * 256, q->scratch, lv, 0);
+      if(rc)
+        return rc;
+      k_radix_scatter<<<nb, kSortBlock, 0, q->stream>>>(q->keys[src], q->vals[src], cap, total_dev,
+                                                        shift, q->hist, nb, q->keys[src ^ 1],
+                                                        q->vals[src ^ 1]);
+      q->launches += 2;
+      src ^= 1;
+    }
+    J.keys = (u64)q->keys[src];
+    J.vals = (u64)q->vals[src];
+    CK(cudaMemcpyAsync(q->status + 1, total_dev, 4, cudaMemcpyDeviceToDevice, q->stream));
+    k_flag_overflow<<<1, 1, 0, q->stream>>>(q->status + 1, cap, q->status);
+    const unsigned rg = std::max(1u, std::min<u32>((cap + 255) / 256, (u32)g_sms * 8));
+    k_ranges<<<rg, 256, 0, q->stream>>>(q->keys[src], q->status + 1, cap, q->tstart, q->tend,
+                                        (uint2 *)q->work, q->status, j.d_targets,
+                                        (u32)j.targets.size());
+    q->launches += 2;
+  }
+  if(j.all_tiles)
+  {
+    launch_clear_empty(q->stream, j, q->tend);
+    q->launches++;
+  }
+  if(!j.num_tris)
+    return VGPU_OK;
+  const unsigned warps = j.var->warps;
+  const unsigned per_sm = g_tuning.raster_blocks_per_sm ? g_tuning.raster_blocks_per_sm
+                                                        : std::max(1u, 32u / warps);
+  unsigned grid = std::max(1u, (unsigned)g_sms * per_sm);
+  grid = std::max(1u, std::min<unsigned>(grid, std::min(j.num_tiles, cap)));
+  const bool timed = g_tuning.time_raster && q->rev_used + 2 <= q->rev.size();
+  if(timed)
+    CK(cudaEventRecordWithFlags(q->rev[q->rev_used], q->stream, cudaEventRecordExternal));
+  int rc = launch(q, j.var->raster, grid, warps * 32, &J);
+  if(timed)
+  {
+    CK(cudaEventRecordWithFlags(q->rev[q->rev_used + 1], q->stream, cudaEventRecordExternal));
+    q->rev_used += 2;
+  }
+  return rc;
+}
+
+/* Capture the whole submission of a list into a CUDA graph on q's stream. */
+static int capture_graph(vgpu_queue *q, vgpu_list *l)
+{
+  graph_forget(l);
+  std::vector<u32> cap(l->jobs.size(), 0);
+  u32 maxcap = 0, maxtiles = 0, rasters = 0;
+  u64 scratch = 0, pairs = 0;
+  for(size_t i = 0; i < l->jobs.size(); i++)
+  {
+    const Job &j = l->jobs[i];
+    cap[i] = graph_capacity(j, l->h_totals[i]);
+    pairs += l->h_totals[i];
+    maxcap = std::max(maxcap, cap[i]);
+    maxtiles = std::max(maxtiles, j.num_tiles);
+    rasters += j.num_tris ? 1 : 0;
+    std::vector<u64> lv;
+    u64 need = 0;
+    hist_levels(cap[i], lv, need);
+    scratch = std::max(scratch, need + 4);
+  }
+  /* every allocation happens before the capture */
+  int rc = ensure_pairs(q, maxcap);
+  if(!rc)
+    rc = ensure_tiles(q, maxtiles);
+  if(!rc)
+    rc = ensure_scratch(q, scratch);
+  if(rc)
+    return rc;
+  if(!l->h_gstatus)
+    CK(cudaMallocHost(&l->h_gstatus, sizeof(u32)));
+  *l->h_gstatus = 0;
+  while(q->rev.size() < 2 * (size_t)rasters)
+  {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    q->rev.push_back(e);
+  }
+  CK(cudaStreamSynchronize(q->stream));
+  const u64 launches0 = q->launches;
+  q->rev_used = 0;
+  CK(cudaStreamBeginCapture(q->stream, cudaStreamCaptureModeThreadLocal));
+  rc = VGPU_OK;
+  auto rec = [&](cudaError_t e) {
+    if(e != cudaSuccess && rc == VGPU_OK)
+      rc = VGPU_ERROR_INITIALIZATION_FAILED;
+  };
+  rec(cudaEventRecordWithFlags(q->ev0, q->stream, cudaEventRecordExternal));
+  for(auto &u : l->uploads)
+    rec(cudaMemcpyAsync(u.first, u.second.first, u.second.second, cudaMemcpyHostToDevice, q->stream));
+  size_t p = 0;
+  while(rc == VGPU_OK && p < l->plan.size())
+  {
+    size_t e = p;
+    while(e < l->plan.size() && l->plan[e].kind != Exec::E_SEGMENT_END &&
+          l->plan[e].kind != Exec::E_COPY)
+      e++;
+    for(size_t i = p; i < e && rc == VGPU_OK; i++)
+      if(l->plan[i].kind == Exec::E_JOB)
+        rc = run_setup(q, l, l->plan[i].index);
+    for(size_t i = p; i < e && rc == VGPU_OK; i++)
+    {
+      const Exec &x = l->plan[i];
+      if(x.kind == Exec::E_CLEAR)
+      {
+        u64 n = (u64)x.target.width * x.target.height;
+        unsigned g = (unsigned)std::min<u64>((n + 255) / 256, (u64)g_sms * 16);
+        k_clear<<<std::max(g, 1u), 256, 0, q->stream>>>(x.target, x.color, x.depth);
+        q->launches++;
+      }
+      else if(x.kind == Exec::E_JOB)
+      {
+        rc = record_raster_fixed(q, l, x.index, cap[x.index]);
+      }
+    }
+    if(rc == VGPU_OK && e < l->plan.size() && l->plan[e].kind == Exec::E_COPY)
+    {
+      const Cmd &c = l->cmds[l->plan[e].index];
+      rec(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, q->stream));
+    }
+    p = e + 1;
+  }
+  for(auto &d : l->downloads)
+    rec(cudaMemcpyAsync(d.first, d.second.first, d.second.second, cudaMemcpyDeviceToHost, q->stream));
+  rec(cudaMemcpyAsync(l->h_gstatus, q->status, sizeof(u32), cudaMemcpyDeviceToHost, q->stream));
+  rec(cudaEventRecordWithFlags(q->ev1, q->stream, cudaEventRecordExternal));
+  cudaGraph_t g = nullptr;
+  cudaError_t ee = cudaStreamEndCapture(q->stream, &g);
+  if(ee == cudaSuccess && rc == VGPU_OK && g)
+    ee = cudaGraphInstantiate(&l->gexec, g, 0);
+  if(g)
+    cudaGraphDestroy(g);
+  const u64 captured = q->launches - launches0;
+  q->launches = launches0;
+  if(ee != cudaSuccess || rc != VGPU_OK)
+  {
+    cudaGetLastError();
+    l->gexec = nullptr;
+    return rc != VGPU_OK ? rc : VGPU_ERROR_INITIALIZATION_FAILED;
+  }
+  l->gq = q;
+  l->g_buf_gen = q->buf_gen;
+  l->g_launches = captured;
+  l->g_pairs = pairs;
+  l->g_rev = q->rev_used;
+  return VGPU_OK;
+}
+
+static int submit_graph(vgpu_queue *q, vgpu_list *l)
+{
+  if(!l->gexec || l->gq != q || l->g_buf_gen != q->buf_gen)
+  {
+    int rc = capture_graph(q, l);
+    if(rc)
+    {
+      /* capture refused (for instance inside a caller's own capture): plain path */
+      graph_forget(l);
+      return submit_plain(q, l);
+    }
+  }
+  CK(cudaGraphLaunch(l->gexec, q->stream));
+  q->stats.graph_replays++;
+  q->launches += l->g_launches;
+  q->rev_used = l->g_rev;
+  q->timed = true;
+  q->stats.tris_in += l->tris_in;
+  q->stats.pairs += l->g_pairs;
+  for(const Cmd &c : l->cmds)
+    if(c.type == CMD_DRAW)
+      q->stats.draws++;
+  q->stats.jobs += l->jobs.size();
+  if(std::find(q->gpending.begin(), q->gpending.end(), l) == q->gpending.end())
+    q->gpending.push_back(l);
+  return VGPU_OK;
+}
+
+/* After the queue's work has completed: a graph replay whose geometry
+   outgrew its pair capacity rasterised nothing; submit that list again with
+   exact storage (the next replay captures a larger graph). */
+static int resolve_pending(vgpu_queue *q)
+{
+  std::lock_guard<std::recursive_mutex> lk(q->mu);
+  if(q->gpending.empty())
+    return VGPU_OK;
+  std::vector<vgpu_list *> todo;
+  todo.swap(q->gpending);
+  for(vgpu_list *l : todo)
+  {
+    if(!l->h_gstatus || !(*l->h_gstatus & VGX_STATUS_PAIR_OVERFLOW))
+      continue;
+    *l->h_gstatus = 0;
+    graph_forget(l);
+    q->stats.graph_reruns++;
+    CK(cudaMemsetAsync(q->status, 0, 4, q->stream));
+    int rc = submit_plain(q, l);
+    if(rc)
+      return rc;
+    CK(cudaStreamSynchronize(q->stream));
+  }
+  return VGPU_OK;
+}
+
+extern "C" int vgpu_submit(vgpu_queue *q, vgpu_list *l)
+{
+  std::lock_guard<std::recursive_mutex> lk(q->mu);
+  if(!l->built || l->built_gen != g_tuning_gen)
+  {
+    int rc = list_build(l);
+    if(rc)
+      return rc;
+  }
+  if(g_tuning.use_graphs && l->mode == VGPU_MODE_BATCHED && l->have_totals)
+    return submit_graph(q, l);
+  int rc = submit_plain(q, l);
+  if(rc == VGPU_OK)
+    l->have_totals = true;
+  return rc;
+}
+
 extern "C" int vgpu_fence_create(vgpu_fence **out)
 {
   int rc = vgpu_init();
@@ -1531,6 +1846,16 @@ extern "C" int vgpu_fence_status(vgpu_fence *f)
     return VGPU_TIMEOUT;
   if(e != cudaSuccess)
     return VGPU_ERROR_DEVICE_LOST;
+  if(f->q && !f->q->gpending.empty())
+  {
+    /* graph replays are checked for pair overflow once the whole queue is idle */
+    e = cudaStreamQuery(f->q->stream);
+    if(e == cudaErrorNotReady)
+      return VGPU_TIMEOUT;
+    if(e != cudaSuccess)
+      return VGPU_ERROR_DEVICE_LOST;
+    return resolve_pending(f->q);
+  }
   return VGPU_OK;
 }
 
@@ -1541,6 +1866,11 @@ extern "C" int vgpu_fence_wait(vgpu_fence *f, uint64_t timeout_ns)
   if(timeout_ns == ~0ull)
   {
     CK(cudaEventSynchronize(f->ev));
+    if(f->q && !f->q->gpending.empty())
+    {
+      CK(cudaStreamSynchronize(f->q->stream));
+      return resolve_pending(f->q);
+    }
     return VGPU_OK;
   }
   struct timespec t0, t1;
@@ -1570,12 +1900,15 @@ extern "C" void vgpu_fence_destroy(vgpu_fence *f)
 extern "C" int vgpu_queue_wait_idle(vgpu_queue *q)
 {
   CK(cudaStreamSynchronize(q->stream));
-  return VGPU_OK;
+  return resolve_pending(q);
 }
 
 extern "C" int vgpu_queue_stats(vgpu_queue *q, vgpu_stats *out)
 {
   CK(cudaStreamSynchronize(q->stream));
+  int rrc = resolve_pending(q);
+  if(rrc)
+    return rrc;
   u64 c[8];
   CK(cudaMemcpy(c, q->counters, sizeof(c), cudaMemcpyDeviceToHost));
   u32 st = 0;
@@ -1747,12 +2080,13 @@ static int run_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, const FixedB
       return VGPU_ERROR_OUT_OF_DEVICE_MEMORY;
     for(u32 shift = 0; shift < j.key_bits; shift += 8)
     {
-      k_radix_hist<<<nb, kSortBlock, 0, q->stream>>>(b.keys[src], total, shift, b.hist, nb);
+      k_radix_hist<<<nb, kSortBlock, 0, q->stream>>>(b.keys[src], total, nullptr, shift, b.hist, nb);
       int rc = scan_u32(q, b.hist, b.hist, n, b.scan, lv, 0);
       if(rc)
         return rc;
-      k_radix_scatter<<<nb, kSortBlock, 0, q->stream>>>(b.keys[src], b.vals[src], total, shift,
-                                                        b.hist, nb, b.keys[src ^ 1], b.vals[src ^ 1]);
+      k_radix_scatter<<<nb, kSortBlock, 0, q->stream>>>(b.keys[src], b.vals[src], total, nullptr,
+                                                        shift, b.hist, nb, b.keys[src ^ 1],
+                                                        b.vals[src ^ 1]);
       q->launches += 2;
       src ^= 1;
     }

@@ -789,6 +789,12 @@ extern "C" void *vsd_queue(vsd_context *c) { return (void *)c->queue; }
 
 extern "C" void *vsd_command_buffer(vsd_scene *s) { return (void *)s->cmd; }
 
+extern "C" int vsd_refresh_vertices(vsd_scene *s)
+{
+  const vsc_scene *sc = s->scene;
+  return sc->vb_bytes ? fill_memory(s->ctx, &s->vb_stage_mem, sc->vb, sc->vb_bytes) : 0;
+}
+
 extern "C" int vsd_request(vsd_scene *s, uint32_t draw, void *out)
 {
 #ifdef VISOR_DRIVER_KHRONOS_HEADER
