@@ -176,7 +176,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     kind = "port"
     o = loader.Oracle()
-    h = o.generate(2, SEED)
+    h = o.generate(2, SEED, **({"count": args.triangles} if args.triangles else {}))
     for _ in range(args.warmup):
         o.render(h, threads=threads)
     times, shaded, tris = [], 0, 0
