@@ -448,15 +448,17 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
       const u32 colmask = (0xffu >> (8 - cx1)) & (0xffu << cx0);
       for(int dy = ry0; dy < ry1; dy++)
       {
-        int q0 = e0 + b0 * dy, q1 = e1 + b1 * dy, q2 = e2 + b2 * dy;
+        /* walk the row from dx = 7 down to 0, shifting each pixel's inside bit
+           (all three edge values non-negative) in at bit 0 */
+        int q0 = e0 + b0 * dy + 7 * a0, q1 = e1 + b1 * dy + 7 * a1, q2 = e2 + b2 * dy + 7 * a2;
         u32 row = 0;
 #pragma unroll
-        for(int dx = 0; dx < 8; dx++)
+        for(int dx = 7; dx >= 0; dx--)
         {
-          row |= ((u32)(~(q0 | q1 | q2)) >> 31) << dx;
-          q0 += a0;
-          q1 += a1;
-          q2 += a2;
+          row = __funnelshift_l(~(u32)(q0 | q1 | q2), row, 1);
+          q0 -= a0;
+          q1 -= a1;
+          q2 -= a2;
         }
         row &= colmask;
         if(dy < 4)
@@ -472,6 +474,34 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     const float margin = mag * 2.0e-6f + 1.0e-30f; /* > the rounding of pixdepth (~4e-7 relative) */
     dlo = fminf(d0, fminf(d1, d2)) - margin;
     dhi = fmaxf(d0, fmaxf(d1, d2)) + margin;
+    if(finite && cx0 < cx1 && ry0 < ry1)
+    {
+      /* Tighter bound over this sub-tile: with exact barycentrics the depth is affine
+         in (x, y), so over the covered part of the clipped rectangle it lies between
+         its values at the rectangle's corners.  Each corner value is computed like a
+         pixel's and widened by its own rounding bound (1e-6 of the sum of the terms'
+         magnitudes, which grows outside the triangle), the pixels' rounding by margin. */
+      const float ia = __int_as_float(r[R_INVAREA]);
+      float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+#pragma unroll
+      for(int c = 0; c < 4; c++)
+      {
+        const int dx = (c & 1) ? cx1 - 1 : cx0, dy = (c & 2) ? ry1 - 1 : ry0;
+        const float n0 = (float)(e0 + a0 * dx + b0 * dy) * ia;
+        const float n1 = (float)(e1 + a1 * dx + b1 * dy) * ia;
+        const float n2 = (float)(e2 + a2 * dx + b2 * dy) * ia;
+        const float t0 = n0 * d0, t1 = n1 * d1, t2 = n2 * d2;
+        const float z = t0 + t1 + t2;
+        const float w = (fabsf(t0) + fabsf(t1) + fabsf(t2)) * 1.0e-6f;
+        lo = fminf(lo, z - w);
+        hi = fmaxf(hi, z + w);
+      }
+      if(isfinite(lo) && isfinite(hi))
+      {
+        dlo = fmaxf(dlo, lo - margin);
+        dhi = fminf(dhi, hi + margin);
+      }
+    }
   }
   covered_total += __popc(mlo) + __popc(mhi);
 
