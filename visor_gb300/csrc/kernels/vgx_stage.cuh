@@ -34,6 +34,10 @@
 #ifndef VGX_RASTER_WARPS
 #define VGX_RASTER_WARPS 1
 #endif
+/* 1: no draw of the job blends, so each pixel shades only its last passing fragment */
+#ifndef VGX_DEFERRED
+#define VGX_DEFERRED 0
+#endif
 #define VGX_SUB_EDGE (1 << (VGX_TILE_SHIFT - 3))
 #define VGX_SUBS (VGX_SUB_EDGE * VGX_SUB_EDGE)
 #define VGX_SUBS_PER_WARP ((VGX_SUBS + VGX_RASTER_WARPS - 1) / VGX_RASTER_WARPS)
@@ -386,7 +390,8 @@ struct VgxWarpShared
 {
   uint4 pe[32], pa[32], pb[32], pd[32];
   float4 col[32];
-  u32 frag[32]; /* fragment window: triangle | pixel-half << 5 | owner lane << 6 */
+  u32 frag[32]; /* fragment window: triangle | pixel-half << 5 | owner lane << 6 (deferred: record) */
+  u32 fown[32]; /* deferred window: owner lane | pixel-half << 5 */
 };
 
 __device__ __forceinline__ VgxPlane vgx_plane_load(const VgxWarpShared &sh, u32 t)
@@ -407,7 +412,7 @@ __device__ __forceinline__ VgxPlane vgx_plane_load(const VgxWarpShared &sh, u32 
  */
 __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShared &sh, int lane,
                                                   u32 n, const int *r, u32 rec_index, int x0, int y0,
-                                                  const bool *in, u32 *col, float *dep,
+                                                  const bool *in, u32 *col, float *dep, u32 *vis,
                                                   u64 &covered_total, u64 &shaded_total,
                                                   u64 &tested_total)
 {
@@ -581,6 +586,13 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     }
   }
   shaded_total += __popc(pass[0]) + __popc(pass[1]);
+#if VGX_DEFERRED
+  /* deferred: the pixel keeps only its last passing fragment; shaded at the bin's end */
+#pragma unroll
+  for(int p = 0; p < 2; p++)
+    if(pass[p])
+      vis[p] = sh.pb[31 - __clz(pass[p])].w;
+#else
   /* Without blending a fragment replaces the pixel's colour bytes (the alpha byte is
      never written, rasterizer.cpp:674-676) and shaders have no side effects, so only
      a pixel's last passing opaque fragment of the batch and the ones after it can
@@ -683,7 +695,88 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     }
     __syncwarp();
   }
+#endif
 }
+
+#if VGX_DEFERRED
+/*
+ * Deferred shading of one 8x8 sub-tile of an all-opaque job: every pixel with a
+ * passing fragment shades it once, in windows of 32 fragments (one per lane),
+ * and the owner lane writes the colour bytes.  Barycentrics are evaluated from
+ * the triangle record exactly as rasterizer.cpp:303-309 does.
+ */
+__device__ __forceinline__ void vgx_shade_deferred(const VgxJob &job, VgxWarpShared &sh, int lane,
+                                                   int x0, int y0, const u32 *vis, u32 *col)
+{
+  const VgxDraw *draws = (const VgxDraw *)job.draws;
+  const u32 mine = (vis[0] != 0xffffffffu ? 1u : 0u) + (vis[1] != 0xffffffffu ? 1u : 0u);
+  u32 incl = mine;
+#pragma unroll
+  for(int o = 1; o < 32; o <<= 1)
+  {
+    u32 v = __shfl_up_sync(0xffffffffu, incl, o);
+    if(lane >= o)
+      incl += v;
+  }
+  const u32 total = __shfl_sync(0xffffffffu, incl, 31);
+  const u32 excl = incl - mine;
+  for(u32 chunk = 0; chunk < total; chunk += 32)
+  {
+    u32 k = excl;
+#pragma unroll
+    for(int p = 0; p < 2; p++)
+      if(vis[p] != 0xffffffffu)
+      {
+        if(k >= chunk && k < chunk + 32)
+        {
+          sh.frag[k - chunk] = vis[p];
+          sh.fown[k - chunk] = (u32)lane | ((u32)p << 5);
+        }
+        k++;
+      }
+    __syncwarp();
+    if(chunk + lane < total)
+    {
+      const u32 rec = sh.frag[lane], own = sh.fown[lane];
+      const int px = x0 + (int)(own & 7), py = y0 + (int)((own >> 3) & 3) + 4 * (int)(own >> 5);
+      const u32 *g = (const u32 *)job.records + (u64)rec * VGX_REC;
+      int b0, b1, b2;
+      vgx_bary(g, px, py, b0, b1, b2);
+      const float ia = __uint_as_float(__ldg(g + R_INVAREA));
+      float nb[4];
+      nb[0] = (float)b0 * ia;
+      nb[1] = (float)b1 * ia;
+      nb[2] = (float)b2 * ia;
+      /* perspective correction, rasterizer.cpp:580-588 */
+      nb[0] = nb[0] * __uint_as_float(__ldg(g + R_INVW));
+      nb[1] = nb[1] * __uint_as_float(__ldg(g + R_INVW + 1));
+      nb[2] = nb[2] * __uint_as_float(__ldg(g + R_INVW + 2));
+      const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
+      nb[0] = nb[0] * invlen;
+      nb[1] = nb[1] * invlen;
+      nb[2] = nb[2] * invlen;
+      nb[3] = 0.0f;
+      float iv[3 * (VGX_K > 0 ? VGX_K : 1)];
+#pragma unroll
+      for(int q = 0; q < 3 * VGX_K; q++)
+        iv[q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + q));
+      sh.col[lane] = vgx_fs(draws[__ldg(g + R_DRAW)], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
+                            __uint_as_float(__ldg(g + R_LOD)));
+    }
+    __syncwarp();
+    k = excl;
+#pragma unroll
+    for(int p = 0; p < 2; p++)
+      if(vis[p] != 0xffffffffu)
+      {
+        if(k >= chunk && k < chunk + 32)
+          col[p] = vgx_blend_write(0u, sh.col[k - chunk], col[p]);
+        k++;
+      }
+    __syncwarp();
+  }
+}
+#endif
 
 /*
  * Persistent raster: each CTA takes a bin tile from the queue; warp w owns the
@@ -742,6 +835,7 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
     bool in[VGX_SUBS_PER_WARP][2];
     u32 col[VGX_SUBS_PER_WARP][2];
     float dep[VGX_SUBS_PER_WARP][2];
+    u32 vis[VGX_SUBS_PER_WARP][2]; /* deferred fragment (record) per pixel, all-opaque jobs */
 #pragma unroll
     for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
     {
@@ -752,6 +846,7 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
 #pragma unroll
       for(int p = 0; p < 2; p++)
       {
+        vis[j][p] = 0xffffffffu;
         const int x = sx[j] + ldx, y = sy[j] + ldy + 4 * p;
         in[j][p] = valid[j] && x < T.width && y < T.height;
         const u64 pix = (u64)y * (u32)T.width + (u32)x;
@@ -796,8 +891,14 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
       for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
         if(valid[j])
           vgx_subtile_batch(job, sh, lane, n, r, rec_index, sx[j], sy[j], in[j], col[j], dep[j],
-                            covered_total, shaded_total, tested_total);
+                            vis[j], covered_total, shaded_total, tested_total);
     }
+#if VGX_DEFERRED
+#pragma unroll
+    for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
+      if(valid[j])
+        vgx_shade_deferred(job, sh, lane, sx[j], sy[j], vis[j], col[j]);
+#endif
 
 #pragma unroll
     for(int j = 0; j < VGX_SUBS_PER_WARP; j++)

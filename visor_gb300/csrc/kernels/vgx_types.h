@@ -123,6 +123,8 @@ typedef struct VgxJob {
   u32 tile_shift; /* log2 of the tile edge in pixels */
   u32 key_bits;   /* bits needed for a tile id */
   u32 all_tiles;  /* 1: raster every tile (fused clear), 0: only tiles with triangles */
+  u32 all_opaque; /* 1: no draw of the job blends (each pixel shades only its last fragment) */
+  u32 reserved;
 } VgxJob;
 
 #endif

@@ -547,6 +547,7 @@ struct VgpuVariant
   CUmodule mod = nullptr;
   CUfunction setup = nullptr, raster = nullptr;
   u32 tile_shift = 3, warps = 1;
+  u32 deferred = 0; /* raster shades each pixel's last fragment once (all-opaque jobs) */
 };
 
 struct vgpu_program
@@ -597,11 +598,13 @@ static int compile_cubin(const std::string &src, std::vector<char> &cubin, char 
   return VGPU_OK;
 }
 
-static std::string full_source(const char *shader_source, uint32_t tile_shift, uint32_t warps = 1)
+static std::string full_source(const char *shader_source, uint32_t tile_shift, uint32_t warps = 1,
+                               uint32_t deferred = 0)
 {
   std::string src;
   src += "#define VGX_TILE_SHIFT " + std::to_string(tile_shift) + "\n";
   src += "#define VGX_RASTER_WARPS " + std::to_string(warps) + "\n";
+  src += "#define VGX_DEFERRED " + std::to_string(deferred ? 1 : 0) + "\n";
   src += kVgxTypes;
   src += kVgxDevice;
   src += kVgxTiles;
@@ -614,8 +617,9 @@ extern "C" int vgpu_program_check(const char *shader_source, uint32_t tile_shift
                                   size_t log_size, uint64_t *cubin_bytes)
 {
   std::vector<char> cubin;
-  /* tile_shift carries the warps per bin in bits 8..15 */
-  int rc = compile_cubin(full_source(shader_source, tile_shift & 0xff, std::max(1u, (tile_shift >> 8) & 0xff)),
+  /* tile_shift carries the warps per bin in bits 8..15 and deferred shading in bit 16 */
+  int rc = compile_cubin(full_source(shader_source, tile_shift & 0xff, std::max(1u, (tile_shift >> 8) & 0xff),
+                                     (tile_shift >> 16) & 1),
                          cubin, log, log_size);
   if(cubin_bytes)
     *cubin_bytes = cubin.size();
@@ -672,19 +676,22 @@ static int load_cubin(const std::string &src, std::vector<char> &cubin, char *lo
 
 /* The variant of a program for a bin tile edge of 2^tile_shift pixels and
    `warps` warps per bin; compiled with NVRTC on first use. */
-static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, int *rc_out)
+static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, u32 deferred,
+                                int *rc_out)
 {
   tile_shift = std::min<u32>(std::max<u32>(tile_shift, 3), 6);
   const u32 subs = 1u << (2 * (tile_shift - 3));
   warps = std::max<u32>(1, std::min<u32>(warps, std::min<u32>(subs, 16)));
-  const u32 key = tile_shift << 8 | warps;
+  deferred = deferred ? 1 : 0;
+  const u32 key = deferred << 16 | tile_shift << 8 | warps;
   std::lock_guard<std::mutex> lk(p->mu);
   auto it = p->variants.find(key);
   if(it != p->variants.end())
     return it->second;
   std::vector<char> cubin;
   char log[4096] = {0};
-  int rc = load_cubin(full_source(p->source.c_str(), tile_shift, warps), cubin, log, sizeof(log));
+  int rc = load_cubin(full_source(p->source.c_str(), tile_shift, warps, deferred), cubin, log,
+                      sizeof(log));
   if(rc)
   {
     *rc_out = rc;
@@ -693,6 +700,7 @@ static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, int 
   VgpuVariant *v = new VgpuVariant();
   v->tile_shift = tile_shift;
   v->warps = warps;
+  v->deferred = deferred;
   if(cudaSetDevice(g_device) != cudaSuccess || g_cu.moduleLoadData(&v->mod, cubin.data()) != CUDA_SUCCESS ||
      g_cu.moduleGetFunction(&v->setup, v->mod, "vgx_setup") != CUDA_SUCCESS ||
      g_cu.moduleGetFunction(&v->raster, v->mod, "vgx_raster") != CUDA_SUCCESS)
@@ -720,7 +728,7 @@ extern "C" int vgpu_program_create(const char *shader_source, uint32_t tile_shif
   p->k = (u32)atoi(kd + 14);
   p->rec_words = ((20 + 3 * p->k) + 3) & ~3u;
   /* compile the default variant now, as vkCreateGraphicsPipelines compiles */
-  if(!get_variant(p, tile_shift, g_tuning.raster_warps, &rc))
+  if(!get_variant(p, tile_shift, g_tuning.raster_warps, 0, &rc))
   {
     if(log && log_size)
       snprintf(log, log_size, "stage kernel compilation failed");
@@ -773,7 +781,7 @@ struct Job
   std::vector<VgxDraw> draws;
   std::vector<VgxTarget> targets;
   std::vector<u64> target_keys; /* colour address identifies a target */
-  u32 num_tris = 0, num_tiles = 0, key_bits = 1, all_tiles = 0;
+  u32 num_tris = 0, num_tiles = 0, key_bits = 1, all_tiles = 0, all_opaque = 1;
   /* device */
   VgxDraw *d_draws = nullptr;
   VgxTarget *d_targets = nullptr;
@@ -1008,7 +1016,7 @@ static int list_build(vgpu_list *l)
     if(!open || !batched || !same_code)
     {
       int vrc = VGPU_OK;
-      VgpuVariant *var = get_variant(c.prog, g_tuning.bin_shift, g_tuning.raster_warps, &vrc);
+      VgpuVariant *var = get_variant(c.prog, g_tuning.bin_shift, g_tuning.raster_warps, 0, &vrc);
       if(!var)
         return vrc;
       l->jobs.emplace_back();
@@ -1061,6 +1069,8 @@ static int list_build(vgpu_list *l)
     }
     VgxDraw d = c.draw;
     d.target = tidx;
+    if(d.blend_enable)
+      open->all_opaque = 0;
     d.tri_base = open->num_tris;
     open->num_tris += ntris;
     open->draws.push_back(d);
@@ -1072,6 +1082,15 @@ static int list_build(vgpu_list *l)
   u64 rec_words = 0, cnt_words = 0;
   for(Job &j : l->jobs)
   {
+    if(j.all_opaque && j.num_tris)
+    {
+      /* no draw blends: the raster variant that shades each pixel's last fragment once */
+      int vrc = VGPU_OK;
+      VgpuVariant *dv = get_variant(j.prog, j.var->tile_shift, j.var->warps, 1, &vrc);
+      if(!dv)
+        return vrc;
+      j.var = dv;
+    }
     j.key_bits = bits_for(std::max(j.num_tiles, 2u));
     j.rec_off = rec_words;
     rec_words += (u64)j.num_tris * j.prog->rec_words;
@@ -1326,6 +1345,7 @@ static VgxJob make_job(vgpu_queue *q, vgpu_list *l, Job &j, size_t ji)
   J.tile_shift = j.var->tile_shift;
   J.key_bits = j.key_bits;
   J.all_tiles = j.all_tiles;
+  J.all_opaque = j.all_opaque;
   (void)ji;
   return J;
 }
