@@ -203,6 +203,10 @@ CONFIG_SCENES = {
                                    "flags": vs.FLAG_FILTER_REFERENCE, "textures": 4,
                                    "tex_size": 64}),
     "cfg4_small": (4, 5, {"count": 6, "min_tris": 200, "max_tris": 3000}),
+    # more triangles than pixels: records keep only the header (interpolants recomputed)
+    "cfg3_dense_bilinear": (3, 19, {"width": 96, "height": 64, "count": 12, "min_tris": 1000,
+                                    "max_tris": 4000, "flags": vs.FLAG_FILTER_REFERENCE,
+                                    "textures": 2, "tex_size": 64}),
     "cfg5_request_bilinear": (5, 13, {"count": 2, "max_tris": 20000, "textures": 4,
                                       "tex_size": 128, "flags": vs.FLAG_FILTER_REFERENCE}),
 }

@@ -28,15 +28,23 @@
 #define VGX_TILE_SHIFT 3
 #endif
 #define VGX_TILE (1 << VGX_TILE_SHIFT)
+/* Shading mode.  0: immediate (fragments shaded and blended per batch).  With no
+   blending draw in the job each pixel shades only its last passing fragment at
+   the end of the bin: 1 keeps the interpolants in the triangle records, 2 stores
+   the record header only and runs the vertex shader again for the triangles of
+   the few fragments that are shaded (jobs with more triangles than pixels). */
+#ifndef VGX_DEFERRED
+#define VGX_DEFERRED 0
+#endif
+#if VGX_DEFERRED == 2
+#define VGX_REC VGX_REC_HEAD
+#else
 #define VGX_REC (((VGX_REC_HEAD + 3 * VGX_K) + 3) & ~3)
+#endif
 /* warps per raster CTA; a CTA owns one bin tile of 2^VGX_TILE_SHIFT pixels and
    its warps split it into 8x8 sub-tiles */
 #ifndef VGX_RASTER_WARPS
 #define VGX_RASTER_WARPS 1
-#endif
-/* 1: no draw of the job blends, so each pixel shades only its last passing fragment */
-#ifndef VGX_DEFERRED
-#define VGX_DEFERRED 0
 #endif
 #define VGX_SUB_EDGE (1 << (VGX_TILE_SHIFT - 3))
 #define VGX_SUBS (VGX_SUB_EDGE * VGX_SUB_EDGE)
@@ -80,6 +88,48 @@ __device__ __forceinline__ void vgx_warp_add_u64(u64 *dst, u64 v)
     atomicAdd((unsigned long long *)dst, s);
 }
 
+/* Vertex indices of triangle `local` of a draw (ShadeVerts, rasterizer.cpp:100-232:
+   lists take three consecutive elements, strips swap the first two of odd
+   triangles); returns true when an index lies outside the bound index buffer
+   (its vertex is then vertex 0). */
+__device__ __forceinline__ bool vgx_tri_indices(const VgxDraw &D, u32 local, u32 *idx)
+{
+  u32 vi[3];
+  if(D.topology == VGX_TOPO_STRIP)
+  {
+    vi[0] = (local & 1u) ? local + 1 : local;
+    vi[1] = (local & 1u) ? local : local + 1;
+    vi[2] = local + 2;
+  }
+  else
+  {
+    vi[0] = local * 3;
+    vi[1] = local * 3 + 1;
+    vi[2] = local * 3 + 2;
+  }
+  bool bad = false;
+#pragma unroll
+  for(int k = 0; k < 3; k++)
+  {
+    const u32 e = D.first + vi[k];
+    idx[k] = e;
+    if(D.index_type != VGX_INDEX_NONE)
+    {
+      if((u64)e >= D.ib_count)
+      {
+        bad = true;
+        idx[k] = 0;
+      }
+      else
+      {
+        idx[k] = D.index_type == VGX_INDEX_U16 ? (u32)__ldg((const u16 *)D.ib + e)
+                                               : __ldg((const u32 *)D.ib + e);
+      }
+    }
+  }
+  return bad;
+}
+
 extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
 {
   vgx_init_unorm8();
@@ -95,43 +145,13 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
     const VgxDraw &D = draws[di];
     const VgxTarget T = ((const VgxTarget *)job.targets)[D.target];
     const u32 local = tri - D.tri_base;
-    u32 vi[3];
-    if(D.topology == VGX_TOPO_STRIP)
-    {
-      /* ShadeVerts strip order (rasterizer.cpp:150-232): odd triangles swap the first two */
-      vi[0] = (local & 1u) ? local + 1 : local;
-      vi[1] = (local & 1u) ? local : local + 1;
-      vi[2] = local + 2;
-    }
-    else
-    {
-      vi[0] = local * 3;
-      vi[1] = local * 3 + 1;
-      vi[2] = local * 3 + 2;
-    }
+    u32 vidx[3];
+    const bool bad = vgx_tri_indices(D, local, vidx);
     float4 pos[3];
     float iv[3][VGX_K > 0 ? VGX_K : 1];
-    bool bad = false;
 #pragma unroll
     for(int k = 0; k < 3; k++)
-    {
-      u32 e = D.first + vi[k];
-      u32 idx = e;
-      if(D.index_type != VGX_INDEX_NONE)
-      {
-        if((u64)e >= D.ib_count)
-        {
-          bad = true;
-          idx = 0;
-        }
-        else
-        {
-          idx = D.index_type == VGX_INDEX_U16 ? (u32)__ldg((const u16 *)D.ib + e)
-                                              : __ldg((const u32 *)D.ib + e);
-        }
-      }
-      vgx_vs(D, idx, pos[k], iv[k]);
-    }
+      vgx_vs(D, vidx[k], pos[k], iv[k]);
     if(bad)
       atomicOr((u32 *)job.status, VGX_STATUS_BAD_INDEX);
 
@@ -218,11 +238,13 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
 #pragma unroll
           for(int w = 0; w < VGX_REC_HEAD; w += 4)
             *(uint4 *)(rec + w) = make_uint4(r[w], r[w + 1], r[w + 2], r[w + 3]);
+#if VGX_DEFERRED != 2
 #pragma unroll
           for(int k = 0; k < 3; k++)
 #pragma unroll
             for(int j = 0; j < VGX_K; j++)
               rec[VGX_REC_HEAD + k * VGX_K + j] = __float_as_uint(iv[k][j]);
+#endif
           ntiles = vgx_count_tiles(r);
         }
       }
@@ -756,12 +778,27 @@ __device__ __forceinline__ void vgx_shade_deferred(const VgxJob &job, VgxWarpSha
       nb[1] = nb[1] * invlen;
       nb[2] = nb[2] * invlen;
       nb[3] = 0.0f;
-      float iv[3 * (VGX_K > 0 ? VGX_K : 1)];
+      const VgxDraw &D = draws[__ldg(g + R_DRAW)];
+      float iv[3][VGX_K > 0 ? VGX_K : 1];
+#if VGX_DEFERRED == 2
+      /* the vertex shader again for the triangle's three vertices (deterministic, so
+         the interpolants equal the ones setup computed) */
+      u32 vidx[3];
+      (void)vgx_tri_indices(D, rec - D.tri_base, vidx);
 #pragma unroll
-      for(int q = 0; q < 3 * VGX_K; q++)
-        iv[q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + q));
-      sh.col[lane] = vgx_fs(draws[__ldg(g + R_DRAW)], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
-                            __uint_as_float(__ldg(g + R_LOD)));
+      for(int v = 0; v < 3; v++)
+      {
+        float4 pos;
+        vgx_vs(D, vidx[v], pos, iv[v]);
+      }
+#else
+#pragma unroll
+      for(int v = 0; v < 3; v++)
+#pragma unroll
+        for(int q = 0; q < VGX_K; q++)
+          iv[v][q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + v * VGX_K + q));
+#endif
+      sh.col[lane] = vgx_fs(D, nb, iv[0], iv[1], iv[2], __uint_as_float(__ldg(g + R_LOD)));
     }
     __syncwarp();
     k = excl;

@@ -547,7 +547,8 @@ struct VgpuVariant
   CUmodule mod = nullptr;
   CUfunction setup = nullptr, raster = nullptr;
   u32 tile_shift = 3, warps = 1;
-  u32 deferred = 0; /* raster shades each pixel's last fragment once (all-opaque jobs) */
+  u32 deferred = 0; /* shading mode: 0 immediate, 1/2 each pixel's last fragment once (all-opaque jobs) */
+  u32 rec_words = 0; /* triangle record size: the header only when deferred */
 };
 
 struct vgpu_program
@@ -604,7 +605,7 @@ static std::string full_source(const char *shader_source, uint32_t tile_shift, u
   std::string src;
   src += "#define VGX_TILE_SHIFT " + std::to_string(tile_shift) + "\n";
   src += "#define VGX_RASTER_WARPS " + std::to_string(warps) + "\n";
-  src += "#define VGX_DEFERRED " + std::to_string(deferred ? 1 : 0) + "\n";
+  src += "#define VGX_DEFERRED " + std::to_string(std::min<uint32_t>(deferred, 2)) + "\n";
   src += kVgxTypes;
   src += kVgxDevice;
   src += kVgxTiles;
@@ -617,9 +618,9 @@ extern "C" int vgpu_program_check(const char *shader_source, uint32_t tile_shift
                                   size_t log_size, uint64_t *cubin_bytes)
 {
   std::vector<char> cubin;
-  /* tile_shift carries the warps per bin in bits 8..15 and deferred shading in bit 16 */
+  /* tile_shift carries the warps per bin in bits 8..15 and the shading mode in bits 16..17 */
   int rc = compile_cubin(full_source(shader_source, tile_shift & 0xff, std::max(1u, (tile_shift >> 8) & 0xff),
-                                     (tile_shift >> 16) & 1),
+                                     (tile_shift >> 16) & 3),
                          cubin, log, log_size);
   if(cubin_bytes)
     *cubin_bytes = cubin.size();
@@ -682,7 +683,7 @@ static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, u32 
   tile_shift = std::min<u32>(std::max<u32>(tile_shift, 3), 6);
   const u32 subs = 1u << (2 * (tile_shift - 3));
   warps = std::max<u32>(1, std::min<u32>(warps, std::min<u32>(subs, 16)));
-  deferred = deferred ? 1 : 0;
+  deferred = std::min<u32>(deferred, 2);
   const u32 key = deferred << 16 | tile_shift << 8 | warps;
   std::lock_guard<std::mutex> lk(p->mu);
   auto it = p->variants.find(key);
@@ -701,6 +702,7 @@ static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, u32 
   v->tile_shift = tile_shift;
   v->warps = warps;
   v->deferred = deferred;
+  v->rec_words = deferred == 2 ? 20u : p->rec_words;
   if(cudaSetDevice(g_device) != cudaSuccess || g_cu.moduleLoadData(&v->mod, cubin.data()) != CUDA_SUCCESS ||
      g_cu.moduleGetFunction(&v->setup, v->mod, "vgx_setup") != CUDA_SUCCESS ||
      g_cu.moduleGetFunction(&v->raster, v->mod, "vgx_raster") != CUDA_SUCCESS)
@@ -1084,16 +1086,22 @@ static int list_build(vgpu_list *l)
   {
     if(j.all_opaque && j.num_tris)
     {
-      /* no draw blends: the raster variant that shades each pixel's last fragment once */
+      /* no draw blends: the raster variant that shades each pixel's last fragment once;
+         with more triangles than pixels, records drop the interpolants (recomputed for
+         the shaded fragments) */
+      u64 pixels = 0;
+      for(const VgxTarget &t : j.targets)
+        pixels += (u64)t.width * (u32)t.height;
+      const u32 mode = (u64)j.num_tris > pixels ? 2u : 1u;
       int vrc = VGPU_OK;
-      VgpuVariant *dv = get_variant(j.prog, j.var->tile_shift, j.var->warps, 1, &vrc);
+      VgpuVariant *dv = get_variant(j.prog, j.var->tile_shift, j.var->warps, mode, &vrc);
       if(!dv)
         return vrc;
       j.var = dv;
     }
     j.key_bits = bits_for(std::max(j.num_tiles, 2u));
     j.rec_off = rec_words;
-    rec_words += (u64)j.num_tris * j.prog->rec_words;
+    rec_words += (u64)j.num_tris * j.var->rec_words;
     j.cnt_off = cnt_words;
     cnt_words += (u64)j.num_tris + 1;
     /* scan scratch levels after the counts */
@@ -1413,7 +1421,7 @@ static int run_raster(vgpu_queue *q, vgpu_list *l, size_t ji)
   q->stats.pairs += total;
   if(total)
   {
-    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.prog->rec_words, counts);
+    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.var->rec_words, counts);
     q->launches++;
     /* radix sort by tile id */
     u32 nb = (total + kSortTile - 1) / kSortTile;
@@ -1607,7 +1615,7 @@ static int record_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, u32 cap)
   if(j.num_tris)
   {
     const u32 *total_dev = counts + j.num_tris;
-    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.prog->rec_words, counts);
+    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.var->rec_words, counts);
     q->launches++;
     const u32 nb = (cap + kSortTile - 1) / kSortTile;
     std::vector<u64> lv;
@@ -2084,7 +2092,7 @@ static int run_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, const FixedB
   int src = 0;
   if(total)
   {
-    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.prog->rec_words, counts);
+    k_emit<<<(j.num_tris + 255) / 256, 256, 0, q->stream>>>(J, j.var->rec_words, counts);
     q->launches++;
     const u32 nb = (total + kSortTile - 1) / kSortTile;
     const u64 n = (u64)nb * 256;
