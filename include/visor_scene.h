@@ -33,6 +33,7 @@ enum {
   VSC_SHADER_LAMBERT_TEX = 1,       /* pos/normal/uv; MVP push constant; tex * max(dot(N,L),0) */
   VSC_SHADER_COLOR = 2,             /* clip-space pos + RGBA8 colour; colour pass-through */
   VSC_SHADER_LAMBERT_TEX_ALPHA = 3, /* as LAMBERT_TEX plus a per-vertex alpha written to .w */
+  VSC_SHADER_CUBE = 4,              /* LAMBERT_TEX vertices; samplerCube read at the interpolated normal */
 };
 
 /* Vertex layouts implied by each shader (bytes per vertex). */
@@ -71,10 +72,19 @@ typedef struct vsc_pipeline {
   uint32_t filter;       /* VSC_FILTER_* */
 } vsc_pipeline;
 
+/* texture formats (texture_sampling.cpp:93-118 decodes the block formats) */
+enum {
+  VSC_TEXFMT_RGBA8 = 0, /* VK_FORMAT_R8G8B8A8_UNORM, 4 bytes a texel */
+  VSC_TEXFMT_BC2 = 1,   /* VK_FORMAT_BC2_UNORM_BLOCK, 16 bytes a 4x4 block */
+  VSC_TEXFMT_BC3 = 2,   /* VK_FORMAT_BC3_UNORM_BLOCK, 16 bytes a 4x4 block */
+};
+
 typedef struct vsc_texture {
   uint32_t width, height, mips;
-  uint64_t bytes;   /* all mips, packed as precompiled.cpp:3-36 lays them out */
-  uint8_t *texels;  /* RGBA8 */
+  uint64_t bytes;   /* every layer, each with all mips, packed as precompiled.cpp:3-36 lays them out */
+  uint8_t *texels;  /* RGBA8 texels or BC blocks */
+  uint32_t format;  /* VSC_TEXFMT_* */
+  uint32_t layers;  /* 1, or 6 for a cube map (faces +X -X +Y -Y +Z -Z) */
 } vsc_texture;
 
 typedef struct vsc_target {
@@ -167,6 +177,9 @@ uint32_t vsc_add_target(vsc_scene *s, uint32_t width, uint32_t height);
 uint32_t vsc_add_pipeline(vsc_scene *s, const vsc_pipeline *p);
 uint32_t vsc_add_texture(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
                          const uint8_t *texels /* may be NULL: seeded random mip 0 */, uint64_t seed);
+/* Seeded random contents of any format; RGBA8 mips are box-filtered, block-format mips random. */
+uint32_t vsc_add_texture_fmt(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
+                             uint32_t format, uint32_t layers, uint64_t seed);
 uint64_t vsc_add_vertices(vsc_scene *s, const void *data, uint64_t bytes); /* returns byte offset */
 uint64_t vsc_add_indices(vsc_scene *s, const uint32_t *idx, uint64_t count); /* returns first index */
 uint32_t vsc_add_draw(vsc_scene *s, const vsc_draw *d);
@@ -186,6 +199,10 @@ uint32_t vsc_vertex_attrs(uint32_t shader, vsc_attr *attrs);
 /* Helpers the tests use to describe draws. */
 uint32_t vsc_stride_of(uint32_t shader);
 uint64_t vsc_texture_mip_offset(const vsc_texture *t, uint32_t mip);
+/* Bytes of one layer (all its mips): the stride between cube faces. */
+uint64_t vsc_texture_layer_bytes(const vsc_texture *t);
+/* Bytes a texel occupies in the layout: 4 for RGBA8, 1 for the block formats (images.cpp:26-33). */
+uint32_t vsc_texture_bpp(uint32_t format);
 uint64_t vsc_triangle_count(const vsc_scene *s);
 uint64_t vsc_hash_bytes(const void *p, uint64_t n); /* FNV-1a 64 */
 

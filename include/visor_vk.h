@@ -427,6 +427,11 @@ typedef enum VkImageUsageFlagBits {
   VK_IMAGE_USAGE_FLAG_BITS_MAX_ENUM = 0x7FFFFFFF
 } VkImageUsageFlagBits;
 
+typedef enum VkImageCreateFlagBits {
+  VK_IMAGE_CREATE_CUBE_COMPATIBLE_BIT = 0x00000010,
+  VK_IMAGE_CREATE_FLAG_BITS_MAX_ENUM = 0x7FFFFFFF
+} VkImageCreateFlagBits;
+
 typedef enum VkBufferUsageFlagBits {
   VK_BUFFER_USAGE_TRANSFER_SRC_BIT = 0x00000001,
   VK_BUFFER_USAGE_TRANSFER_DST_BIT = 0x00000002,

@@ -167,6 +167,17 @@ static void fs_lambert_alpha(const GPUState &s, float, const float4 &b, const Ve
 {
   fs_lambert_impl(s, b, tri, o, true);
 }
+/* samplerCube at the interpolated normal: ImageSampleImplicitLod on a Dim=Cube image
+   lowers to sample_cube_wrapped (spirv_compile.cpp:1842-1886, 896) */
+extern "C" void sample_cube_wrapped(float x, float y, float z, VkImage tex, float4 &out);
+static void fs_cube(const GPUState &state, float, const float4 &b, const VertexCacheEntry tri[3], float4 &o)
+{
+  float n[3];
+  for(int i = 0; i < 3; i++)
+    n[i] = bary_dot(b, tri[0].interps[0].v[i], tri[1].interps[0].v[i], tri[2].interps[0].v[i]);
+  VkImage img = state.sets[0]->binds[0].data.imageInfo.imageView->image;
+  sample_cube_wrapped(n[0], n[1], n[2], img, o);
+}
 static void fs_color(const GPUState &, float, const float4 &b, const VertexCacheEntry tri[3], float4 &o)
 {
   for(int i = 0; i < 4; i++)
@@ -196,6 +207,7 @@ LLVMFunction *CompileFunction(const uint32_t *pCode, size_t codeSize)
       {"visor_shader:lambert_tex_alpha.frag", (Shader)&fs_lambert_alpha},
       {"visor_shader:color.vert", (Shader)&vs_color},
       {"visor_shader:color.frag", (Shader)&fs_color},
+      {"visor_shader:cube.frag", (Shader)&fs_cube},
   };
   size_t i = 5;
   while(i < codeSize)

@@ -4,6 +4,7 @@
  * it lets oracle/Makefile compile the reference's unmodified sources.
  *
  * - MSVC __declspec spellings map to GCC attributes.
+ * - abs(float) resolves to the float overload, as with MSVC's headers.
  * - sprintf_s(char (&)[N], ...) forwards to snprintf.
  * - BC4Mode/BC5Mode are declared before decompress.h uses them.
  * - microprofile.h is skipped (MICROPROFILE_ONCE) and its macros are given
@@ -23,6 +24,11 @@
 #include <map>
 #include <mutex>
 #include <string>
+
+/* MSVC's headers give the global abs() float overloads (the reference calls
+   abs(float) in sample_cube_wrapped, texture_sampling.cpp:189-191); with
+   libstdc++ the global abs is the int one unless std::abs is brought in. */
+using std::abs;
 
 template <size_t N, typename... Args>
 int sprintf_s(char (&buf)[N], const char *fmt, Args... args)

@@ -120,19 +120,112 @@ static float interp(f4 bary, float a, float b, float c)
 /* texture sampling                                                          */
 /* ------------------------------------------------------------------------ */
 
-static f4 texel(const uint8_t *base, uint32_t width, int x, int y)
+/*
+ * Block-compressed texels (CacheCoord, texture_sampling.cpp:93-118, decoding
+ * with the vendored 3rdparty/decompress.c).  A 4x4 block is 16 bytes; blocks
+ * are stored row by row, width/4 blocks a row.  The colour half (bytes 8..15)
+ * holds two RGB565 endpoints and sixteen 2-bit palette indices.  BC2 carries
+ * sixteen explicit 4-bit alphas (x17); BC3 two alpha endpoints and sixteen
+ * 3-bit indices into an interpolated alpha palette.
+ */
+
+/* RGB565 channel to 8 bits: the decompressor's rounding, t = 255v + 2^(n-1),
+   (t + t/2^n) / 2^n, which is not exact rounding for every v */
+static uint8_t bc_expand(uint32_t v, uint32_t bits)
 {
-  /* CacheCoord fills its cache with float(byte)/255.0f per channel, texture_sampling.cpp:123-133 */
-  const uint8_t *p = base + ((uint64_t)y * width + (uint32_t)x) * 4;
+  const uint32_t t = v * 255u + (1u << (bits - 1));
+  return (uint8_t)((t + (t >> bits)) >> bits);
+}
+
+static uint32_t rd16(const uint8_t *p) { return (uint32_t)p[0] | ((uint32_t)p[1] << 8); }
+static uint32_t rd32(const uint8_t *p) { return rd16(p) | (rd16(p + 2) << 16); }
+
+/* RGBA bytes of texel (x, y) of a BC2 (fmt 1) or BC3 (fmt 2) image */
+static void bc_texel(const uint8_t *base, uint32_t width, uint32_t fmt, int x, int y, uint8_t out[4])
+{
+  const uint8_t *blk = base + ((uint64_t)(y >> 2) * (width >> 2) + (uint32_t)(x >> 2)) * 16;
+  const uint32_t i = (uint32_t)((y & 3) * 4 + (x & 3));
+  const uint32_t c0 = rd16(blk + 8), c1 = rd16(blk + 10);
+  uint8_t e[2][3];
+  const uint32_t ce[2] = {c0, c1};
+  for(int k = 0; k < 2; k++)
+  {
+    e[k][0] = bc_expand(ce[k] >> 11, 5);
+    e[k][1] = bc_expand((ce[k] >> 5) & 63u, 6);
+    e[k][2] = bc_expand(ce[k] & 31u, 5);
+  }
+  const uint32_t code = (rd32(blk + 12) >> (2 * i)) & 3u;
+  /* BC2 keeps BC1's rule (three colours and black when c0 <= c1); BC3 always four */
+  const int four = fmt == VSC_TEXFMT_BC3 || c0 > c1;
+  for(int ch = 0; ch < 3; ch++)
+  {
+    const uint32_t a = e[0][ch], b = e[1][ch];
+    uint32_t v;
+    if(code == 0)
+      v = a;
+    else if(code == 1)
+      v = b;
+    else if(four)
+      v = code == 2 ? (2 * a + b) / 3 : (a + 2 * b) / 3;
+    else
+      v = code == 2 ? (a + b) / 2 : 0;
+    out[ch] = (uint8_t)v;
+  }
+  if(fmt == VSC_TEXFMT_BC2)
+  {
+    out[3] = (uint8_t)(((rd16(blk + 2 * (i >> 2)) >> (4 * (i & 3))) & 15u) * 17u);
+  }
+  else
+  {
+    const uint32_t a0 = blk[0], a1 = blk[1];
+    const uint8_t *ib = blk + 2 + 3 * (i >> 3);
+    const uint32_t bits = (uint32_t)ib[0] | ((uint32_t)ib[1] << 8) | ((uint32_t)ib[2] << 16);
+    const uint32_t ac = (bits >> (3 * (i & 7))) & 7u;
+    uint32_t av;
+    if(ac == 0)
+      av = a0;
+    else if(ac == 1)
+      av = a1;
+    else if(a0 > a1)
+      av = ((8 - ac) * a0 + (ac - 1) * a1) / 7;
+    else if(ac == 6)
+      av = 0;
+    else if(ac == 7)
+      av = 255;
+    else
+      av = ((6 - ac) * a0 + (ac - 1) * a1) / 5;
+    out[3] = (uint8_t)av;
+  }
+}
+
+static f4 texel_fmt(const uint8_t *base, uint32_t width, uint32_t fmt, int x, int y)
+{
+  /* CacheCoord fills its cache with float(byte)/255.0f per channel, texture_sampling.cpp:93-133 */
+  uint8_t b[4];
+  if(fmt == VSC_TEXFMT_BC2 || fmt == VSC_TEXFMT_BC3)
+    bc_texel(base, width, fmt, x, y, b);
+  else
+    memcpy(b, base + ((uint64_t)y * width + (uint32_t)x) * 4, 4);
   f4 t;
   for(int ch = 0; ch < 4; ch++)
-    t.v[ch] = (float)p[ch] / 255.0f;
+    t.v[ch] = (float)b[ch] / 255.0f;
   return t;
 }
 
-/* sample_tex_wrapped, texture_sampling.cpp:139-184 */
+static f4 texel(const uint8_t *base, uint32_t width, int x, int y)
+{
+  return texel_fmt(base, width, VSC_TEXFMT_RGBA8, x, y);
+}
+
 void vor_sample_bilinear(const uint8_t *texels, uint32_t width, uint32_t height, float u, float v,
                          float out[4])
+{
+  vor_sample_bilinear_fmt(texels, width, height, VSC_TEXFMT_RGBA8, u, v, out);
+}
+
+/* sample_tex_wrapped, texture_sampling.cpp:139-184 */
+void vor_sample_bilinear_fmt(const uint8_t *texels, uint32_t width, uint32_t height, uint32_t fmt,
+                             float u, float v, float out[4])
 {
   u = u - floorf(u);
   v = v - floorf(v);
@@ -162,10 +255,10 @@ void vor_sample_bilinear(const uint8_t *texels, uint32_t width, uint32_t height,
   if(iv0 >= (int)height)
     iv0 -= height;
 
-  f4 TL = texel(texels, width, iu0, iv0);
-  f4 TR = texel(texels, width, iu1, iv0);
-  f4 BL = texel(texels, width, iu0, iv1);
-  f4 BR = texel(texels, width, iu1, iv1);
+  f4 TL = texel_fmt(texels, width, fmt, iu0, iv0);
+  f4 TR = texel_fmt(texels, width, fmt, iu1, iv0);
+  f4 BL = texel_fmt(texels, width, fmt, iu0, iv1);
+  f4 BR = texel_fmt(texels, width, fmt, iu1, iv1);
 
   for(int ch = 0; ch < 4; ch++)
   {
@@ -228,14 +321,16 @@ void vor_sample_trilinear(const vsc_texture *tex, float lod, float u, float v, f
   if(w0 < 1) w0 = 1;
   if(h0 < 1) h0 = 1;
   float c0[4];
-  vor_sample_bilinear(tex->texels + vsc_texture_mip_offset(tex, l0), w0, h0, u, v, c0);
+  vor_sample_bilinear_fmt(tex->texels + vsc_texture_mip_offset(tex, l0), w0, h0, tex->format, u, v,
+                          c0);
   if(f > 0.0f)
   {
     uint32_t w1 = tex->width >> l1, h1 = tex->height >> l1;
     if(w1 < 1) w1 = 1;
     if(h1 < 1) h1 = 1;
     float c1[4];
-    vor_sample_bilinear(tex->texels + vsc_texture_mip_offset(tex, l1), w1, h1, u, v, c1);
+    vor_sample_bilinear_fmt(tex->texels + vsc_texture_mip_offset(tex, l1), w1, h1, tex->format, u,
+                            v, c1);
     float g = 1.0f - f;
     for(int ch = 0; ch < 4; ch++)
       out[ch] = c0[ch] * g + c1[ch] * f;
@@ -258,7 +353,7 @@ static void sample_nearest(const vsc_texture *tex, float u, float v, float out[4
     iu -= tex->width;
   if(iv >= (int)tex->height)
     iv -= tex->height;
-  f4 t = texel(tex->texels, tex->width, iu, iv);
+  f4 t = texel_fmt(tex->texels, tex->width, tex->format, iu, iv);
   for(int ch = 0; ch < 4; ch++)
     out[ch] = t.v[ch];
 }
@@ -273,9 +368,39 @@ static f4 sample(const draw_ctx *c, const tri_ctx *t, float u, float v)
   {
     case VSC_FILTER_TRILINEAR: vor_sample_trilinear(c->tex, t->lod, u, v, r.v); break;
     case VSC_FILTER_NEAREST: sample_nearest(c->tex, u, v, r.v); break;
-    default: vor_sample_bilinear(c->tex->texels, c->tex->width, c->tex->height, u, v, r.v); break;
+    default:
+      vor_sample_bilinear_fmt(c->tex->texels, c->tex->width, c->tex->height, c->tex->format, u, v,
+                              r.v);
+      break;
   }
   return r;
+}
+
+/*
+ * sample_cube_wrapped, texture_sampling.cpp:186-250: the major axis picks the
+ * face (tests in this order, a later match replacing an earlier one on ties),
+ * then a bilinear sample of that face's mip 0 at 0.5 * (u / axis + 1).
+ */
+void vor_sample_cube(const vsc_texture *tex, float x, float y, float z, float out[4])
+{
+  const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+  const int px = x > 0.0f, py = y > 0.0f, pz = z > 0.0f;
+  float axis = 0.0f, u = 0.0f, v = 0.0f;
+  uint32_t face = 0;
+  if(px && ax >= ay && ax >= az)
+    axis = ax, u = -z, v = -y, face = 0;
+  if(!px && ax >= ay && ax >= az)
+    axis = ax, u = z, v = -y, face = 1;
+  if(py && ay >= ax && ay >= az)
+    axis = ay, u = x, v = z, face = 2;
+  if(!py && ay >= ax && ay >= az)
+    axis = ay, u = x, v = -z, face = 3;
+  if(pz && az >= ax && az >= ay)
+    axis = az, u = x, v = -y, face = 4;
+  if(!pz && az >= ax && az >= ay)
+    axis = az, u = -x, v = -y, face = 5;
+  vor_sample_bilinear_fmt(tex->texels + vsc_texture_layer_bytes(tex) * face, tex->width, tex->height,
+                          tex->format, 0.5f * (u / axis + 1.0f), 0.5f * (v / axis + 1.0f), out);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -366,6 +491,19 @@ static f4 fs_lambert(const draw_ctx *c, const tri_ctx *t, f4 bary, int with_alph
   return out;
 }
 
+/* FS: colour = texture(cubeTex, in0) with in0 the interpolated, unnormalised normal. */
+static f4 fs_cube(const draw_ctx *c, const tri_ctx *t, f4 bary)
+{
+  const vcache *v = t->v;
+  float n[3];
+  for(int i = 0; i < 3; i++)
+    n[i] = interp(bary, v[0].interps[0].v[i], v[1].interps[0].v[i], v[2].interps[0].v[i]);
+  f4 r = {{0.0f, 0.0f, 0.0f, 0.0f}};
+  if(c->tex)
+    vor_sample_cube(c->tex, n[0], n[1], n[2], r.v);
+  return r;
+}
+
 static f4 fs_color(const tri_ctx *t, f4 bary)
 {
   const vcache *v = t->v;
@@ -380,7 +518,8 @@ static void run_vs(const draw_ctx *c, uint32_t index, vcache *out)
   memset(out, 0, sizeof(*out));
   switch(c->p->shader)
   {
-    case VSC_SHADER_LAMBERT_TEX: vs_lambert(c, index, out, 0); break;
+    case VSC_SHADER_LAMBERT_TEX:
+    case VSC_SHADER_CUBE: vs_lambert(c, index, out, 0); break;
     case VSC_SHADER_LAMBERT_TEX_ALPHA: vs_lambert(c, index, out, 1); break;
     case VSC_SHADER_COLOR: vs_color(c, index, out); break;
     default: break;
@@ -394,6 +533,7 @@ static f4 run_fs(const draw_ctx *c, const tri_ctx *t, f4 bary)
     case VSC_SHADER_LAMBERT_TEX: return fs_lambert(c, t, bary, 0);
     case VSC_SHADER_LAMBERT_TEX_ALPHA: return fs_lambert(c, t, bary, 1);
     case VSC_SHADER_COLOR: return fs_color(t, bary);
+    case VSC_SHADER_CUBE: return fs_cube(c, t, bary);
     default:
     {
       f4 z = {{0, 0, 0, 0}};

@@ -54,6 +54,11 @@ int vor_render_threads(const vsc_scene *scene, uint32_t first, uint32_t count, u
 void vor_sample_bilinear(const uint8_t *texels, uint32_t width, uint32_t height, float u, float v,
                          float out[4]);
 void vor_sample_trilinear(const vsc_texture *tex, float lod, float u, float v, float out[4]);
+/* Bilinear of an RGBA8 (0) or BC2/BC3 (VSC_TEXFMT_*) mip. */
+void vor_sample_bilinear_fmt(const uint8_t *texels, uint32_t width, uint32_t height, uint32_t fmt,
+                             float u, float v, float out[4]);
+/* sample_cube_wrapped: six-layer texture, mip 0 of the face the direction selects. */
+void vor_sample_cube(const vsc_texture *tex, float x, float y, float z, float out[4]);
 float vor_lod(float u0, float v0, float u1, float v1, float u2, float v2, uint32_t width,
               uint32_t height, int area2);
 float vor_log2(float x);

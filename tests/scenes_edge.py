@@ -165,6 +165,92 @@ def texture_wrap(lib):
     return sh
 
 
+IDENTITY = struct.pack("<16f", 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1)
+LIGHT = struct.pack("<4f", 0.0, 0.6, 0.8, 0.0)
+
+
+def _lambert_mesh(lib, s, verts, idx):
+    """32-byte pos/normal/uv vertices and uint32 indices into the scene's buffers."""
+    data = b"".join(struct.pack("<8f", *v) for v in verts)
+    off = lib.vsc_add_vertices(s, data, len(data))
+    ia = np.array(idx, np.uint32)
+    first = lib.vsc_add_indices(s, ia.ctypes.data, len(ia))
+    return off, int(first), len(idx)
+
+
+def bc_quads(lib, fmt):
+    """Lambert quads sampling a 32x32 block-compressed texture (BC2 or BC3) with repeat."""
+    sh = vs.new_scene(lib)
+    s = sh.ptr
+    t = lib.vsc_add_target(s, 96, 80)
+    pi = lib.vsc_add_pipeline(s, vs.make_pipeline(vs.SHADER_LAMBERT_TEX))
+    tex = lib.vsc_add_texture_fmt(s, 32, 32, 1, fmt, 1, 41 + fmt)
+    quads = [((-0.95, -0.9), (0.0, 0.05), (-0.4, -0.3), (1.3, 1.1)),
+             ((0.05, -0.9), (0.95, 0.9), (0.1, 0.2), (2.7, 3.1)),
+             ((-0.95, 0.1), (-0.05, 0.95), (0.0, 0.0), (1.0, 1.0))]
+    verts, idx = [], []
+    for (x0, y0), (x1, y1), (u0, v0), (u1, v1) in quads:
+        b = len(verts)
+        for (x, y, u, v) in ((x0, y0, u0, v0), (x1, y0, u1, v0), (x1, y1, u1, v1), (x0, y1, u0, v1)):
+            verts.append((x, y, 0.5, 0.0, 0.3, 1.0, u, v))
+        idx += [b, b + 1, b + 2, b, b + 2, b + 3]
+    off, first, n = _lambert_mesh(lib, s, verts, idx)
+    di = lib.vsc_add_draw(s, vs.make_draw(pi, n, first, indexed=True, texture=tex, vb_offset=off,
+                                          push=IDENTITY + LIGHT))
+    lib.vsc_add_pass(s, t, 1, di, 1)
+    return sh
+
+
+def cube_sphere(lib, fmt=0):
+    """A sphere whose normals sample a 16x16 cube map: every face and its edges."""
+    sh = vs.new_scene(lib)
+    s = sh.ptr
+    t = lib.vsc_add_target(s, 112, 96)
+    pi = lib.vsc_add_pipeline(s, vs.make_pipeline(vs.SHADER_CUBE))
+    tex = lib.vsc_add_texture_fmt(s, 16, 16, 1, fmt, 6, 57 + fmt)
+    verts, idx = [], []
+    rows, cols = 14, 28
+    for r in range(rows + 1):
+        th = np.pi * r / rows
+        for c in range(cols + 1):
+            ph = 2 * np.pi * c / cols
+            x, y, z = np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)
+            verts.append((0.85 * x, 0.85 * y, 0.5 + 0.4 * z, x, y, z, c / cols, r / rows))
+    for r in range(rows):
+        for c in range(cols):
+            a, b = r * (cols + 1) + c, r * (cols + 1) + c + 1
+            d, e = a + cols + 1, b + cols + 1
+            idx += [a, d, b, b, d, e]
+    off, first, n = _lambert_mesh(lib, s, verts, idx)
+    di = lib.vsc_add_draw(s, vs.make_draw(pi, n, first, indexed=True, texture=tex, vb_offset=off,
+                                          push=IDENTITY + LIGHT))
+    lib.vsc_add_pass(s, t, 1, di, 1)
+    return sh
+
+
+def cube_ties(lib):
+    """Constant normals on the boundaries between faces (|x| = |y|, |x| = |z|, all three
+    equal, and a negative-zero component): the face tests' order decides."""
+    sh = vs.new_scene(lib)
+    s = sh.ptr
+    t = lib.vsc_add_target(s, 64, 64)
+    pi = lib.vsc_add_pipeline(s, vs.make_pipeline(vs.SHADER_CUBE, depth_op=vs.CMP_LEQUAL))
+    tex = lib.vsc_add_texture_fmt(s, 8, 8, 1, 0, 6, 71)
+    normals = [(1.0, 1.0, 0.0), (-1.0, 0.0, -1.0), (0.5, -0.5, 0.5), (-0.0, 0.25, -0.25)]
+    verts, idx = [], []
+    for k, (nx, ny, nz) in enumerate(normals):
+        x0, y0 = -0.95 + 0.95 * (k % 2), -0.95 + 0.95 * (k // 2)
+        b = len(verts)
+        for (x, y) in ((x0, y0), (x0 + 0.9, y0), (x0 + 0.9, y0 + 0.9), (x0, y0 + 0.9)):
+            verts.append((x, y, 0.5, nx, ny, nz, 0.0, 0.0))
+        idx += [b, b + 1, b + 2, b, b + 2, b + 3]
+    off, first, n = _lambert_mesh(lib, s, verts, idx)
+    di = lib.vsc_add_draw(s, vs.make_draw(pi, n, first, indexed=True, texture=tex, vb_offset=off,
+                                          push=IDENTITY + LIGHT))
+    lib.vsc_add_pass(s, t, 1, di, 1)
+    return sh
+
+
 EDGE_SCENES = {
     "degenerate": degenerate,
     "winding_none_ccw": lambda lib: windings(lib, vs.CULL_NONE, vs.FRONT_CCW),
@@ -188,6 +274,11 @@ EDGE_SCENES = {
     "strip": strip,
     "load_pass": load_pass,
     "texture_wrap": texture_wrap,
+    "bc2_quads": lambda lib: bc_quads(lib, vs.TEXFMT_BC2),
+    "bc3_quads": lambda lib: bc_quads(lib, vs.TEXFMT_BC3),
+    "cube_sphere": cube_sphere,
+    "cube_sphere_bc3": lambda lib: cube_sphere(lib, vs.TEXFMT_BC3),
+    "cube_ties": cube_ties,
 }
 
 # Generated configurations pinned by fixtures: name -> (config, seed, params)

@@ -1248,6 +1248,11 @@ void fill_texture(VgxTex &t, VkDescriptorSet_T::Bind *b)
     t.mip_offset[m] = (u32)off;
     off += (u64)std::max(1u, t.width >> m) * std::max(1u, t.height >> m) * img->bpp;
   }
+  t.format = img->format == VK_FORMAT_BC2_UNORM_BLOCK   ? VGX_TEX_BC2
+             : img->format == VK_FORMAT_BC3_UNORM_BLOCK ? VGX_TEX_BC3
+                                                        : VGX_TEX_RGBA8;
+  t.layers = img->layers;
+  t.layer_bytes = subresource_offset(img, 0, 1);
 }
 
 /* Pipeline state, vertex attributes, sampled images and uniform buffers of a

@@ -38,6 +38,28 @@ __device__ __forceinline__ float4 vgx_fetch(const VgxDraw &D, u32 loc, u32 index
   if(off + size > D.vb_bytes[a.binding])
     return out;
   const u32 *p = (const u32 *)(D.vb[a.binding] + off);
+  const u64 addr = D.vb[a.binding] + off;
+  /* one wide load where the address is aligned and the wider read stays in the buffer */
+  if(a.format != VGX_FMT_RGBA8_UNORM && a.format != VGX_FMT_R32 && (addr & 15u) == 0 &&
+     off + 16 <= D.vb_bytes[a.binding])
+  {
+    const float4 v = __ldg((const float4 *)p);
+    out.x = v.x;
+    if(a.format != VGX_FMT_R32)
+      out.y = v.y;
+    if(a.format == VGX_FMT_RGB32 || a.format == VGX_FMT_RGBA32)
+      out.z = v.z;
+    if(a.format == VGX_FMT_RGBA32)
+      out.w = v.w;
+    return out;
+  }
+  if(a.format == VGX_FMT_RG32 && (addr & 7u) == 0)
+  {
+    const float2 v = __ldg((const float2 *)p);
+    out.x = v.x;
+    out.y = v.y;
+    return out;
+  }
   switch(a.format)
   {
     case VGX_FMT_RGBA32: out.w = __uint_as_float(__ldg(p + 3)); /* fall through */
@@ -58,9 +80,105 @@ __device__ __forceinline__ float4 vgx_fetch(const VgxDraw &D, u32 loc, u32 index
   return out;
 }
 
-__device__ __forceinline__ float4 vgx_texel(const u8 *base, u32 width, int x, int y)
+#if VGX_TEX_BLOCKS
+/* RGB565 channel to 8 bits with the block decompressor's rounding (texture_sampling.cpp:93-118
+   uses 3rdparty/decompress.c): t = 255v + 2^(n-1), (t + t/2^n) / 2^n */
+__device__ __forceinline__ u32 vgx_bc_expand(u32 v, u32 bits)
 {
-  u32 t = __ldg((const u32 *)(base + ((u64)y * width + (u32)x) * 4u));
+  const u32 t = v * 255u + (1u << (bits - 1));
+  return (t + (t >> bits)) >> bits;
+}
+
+/*
+ * Texel (x, y) of a BC2/BC3 image as RGBA bytes (R in the low byte): 16-byte
+ * 4x4 blocks stored row by row, width/4 a row.  Bytes 8..15 hold two RGB565
+ * endpoints and 2-bit palette indices; BC2 keeps the three-colour palette of
+ * BC1 when c0 <= c1, BC3 always uses four colours.  BC2 alpha: explicit 4 bits
+ * x 17; BC3 alpha: two endpoints and 3-bit indices into 8 (a0 > a1) or 6 + {0,
+ * 255} interpolated values, divisions truncating.  Compiled only into the
+ * raster variants of jobs that bind a block-compressed texture (VGX_TEX_BLOCKS).
+ */
+__device__ __forceinline__ u32 vgx_bc_texel(const u8 *base, u32 width, u32 fmt, int x, int y)
+{
+  const u8 *blk = base + ((u64)(y >> 2) * (width >> 2) + (u32)(x >> 2)) * 16u;
+  uint4 b;
+  if(((u64)blk & 15u) == 0)
+  {
+    b = __ldg((const uint4 *)blk);
+  }
+  else
+  {
+    u32 w[4];
+#pragma unroll
+    for(int k = 0; k < 4; k++)
+      w[k] = (u32)__ldg(blk + 4 * k) | ((u32)__ldg(blk + 4 * k + 1) << 8) |
+             ((u32)__ldg(blk + 4 * k + 2) << 16) | ((u32)__ldg(blk + 4 * k + 3) << 24);
+    b = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  const u32 i = (u32)((y & 3) * 4 + (x & 3));
+  const u32 c0 = b.z & 0xffffu, c1 = b.z >> 16;
+  const u32 code = (b.w >> (2 * i)) & 3u;
+  const bool four = fmt == VGX_TEX_BC3 || c0 > c1;
+  u32 rgb = 0;
+#pragma unroll
+  for(int ch = 0; ch < 3; ch++)
+  {
+    const u32 sh = ch == 0 ? 11u : ch == 1 ? 5u : 0u, bits = ch == 1 ? 6u : 5u;
+    const u32 a = vgx_bc_expand((c0 >> sh) & ((1u << bits) - 1u), bits);
+    const u32 e = vgx_bc_expand((c1 >> sh) & ((1u << bits) - 1u), bits);
+    u32 v;
+    if(code == 0)
+      v = a;
+    else if(code == 1)
+      v = e;
+    else if(four)
+      v = code == 2 ? (2 * a + e) / 3 : (a + 2 * e) / 3;
+    else
+      v = code == 2 ? (a + e) / 2 : 0u;
+    rgb |= v << (8 * ch);
+  }
+  u32 alpha;
+  if(fmt == VGX_TEX_BC2)
+  {
+    const u32 row = i < 8 ? b.x : b.y;
+    alpha = ((row >> (4 * (i & 7))) & 15u) * 17u;
+  }
+  else
+  {
+    const u32 a0 = b.x & 0xffu, a1 = (b.x >> 8) & 0xffu;
+    /* 3-bit indices: bytes 2..4 for texels 0..7, bytes 5..7 for texels 8..15 */
+    const u32 bits = i < 8 ? (b.x >> 16) | ((b.y & 0xffu) << 16) : (b.y >> 8);
+    const u32 ac = (bits >> (3 * (i & 7))) & 7u;
+    if(ac == 0)
+      alpha = a0;
+    else if(ac == 1)
+      alpha = a1;
+    else if(a0 > a1)
+      alpha = ((8 - ac) * a0 + (ac - 1) * a1) / 7;
+    else if(ac == 6)
+      alpha = 0;
+    else if(ac == 7)
+      alpha = 255;
+    else
+      alpha = ((6 - ac) * a0 + (ac - 1) * a1) / 5;
+  }
+  return rgb | (alpha << 24);
+}
+#endif
+
+#ifndef VGX_TEX_BLOCKS
+#define VGX_TEX_BLOCKS 0
+#endif
+
+__device__ __forceinline__ float4 vgx_texel(const u8 *base, u32 width, u32 fmt, int x, int y)
+{
+#if VGX_TEX_BLOCKS
+  const u32 t = fmt == VGX_TEX_RGBA8 ? __ldg((const u32 *)(base + ((u64)y * width + (u32)x) * 4u))
+                                     : vgx_bc_texel(base, width, fmt, x, y);
+#else
+  (void)fmt;
+  const u32 t = __ldg((const u32 *)(base + ((u64)y * width + (u32)x) * 4u));
+#endif
   return make_float4(vgx_unorm8[t & 0xffu], vgx_unorm8[(t >> 8) & 0xffu],
                      vgx_unorm8[(t >> 16) & 0xffu], vgx_unorm8[t >> 24]);
 }
@@ -72,7 +190,7 @@ __device__ __forceinline__ float4 vgx_texel(const u8 *base, u32 width, int x, in
  * the oracle) wraps that texel.  Indices are clamped so NaN/inf coordinates
  * cannot address outside the image.
  */
-__device__ __forceinline__ float4 vgx_bilinear(const u8 *base, u32 W, u32 H, float u, float v)
+__device__ __forceinline__ float4 vgx_bilinear(const u8 *base, u32 W, u32 H, u32 fmt, float u, float v)
 {
   u = u - floorf(u);
   v = v - floorf(v);
@@ -98,10 +216,10 @@ __device__ __forceinline__ float4 vgx_bilinear(const u8 *base, u32 W, u32 H, flo
   iv0 = min(max(iv0, 0), (int)H - 1);
   iu1 = min(max(iu1, 0), (int)W - 1);
   iv1 = min(max(iv1, 0), (int)H - 1);
-  float4 TL = vgx_texel(base, W, iu0, iv0);
-  float4 TR = vgx_texel(base, W, iu1, iv0);
-  float4 BL = vgx_texel(base, W, iu0, iv1);
-  float4 BR = vgx_texel(base, W, iu1, iv1);
+  float4 TL = vgx_texel(base, W, fmt, iu0, iv0);
+  float4 TR = vgx_texel(base, W, fmt, iu1, iv0);
+  float4 BL = vgx_texel(base, W, fmt, iu0, iv1);
+  float4 BR = vgx_texel(base, W, fmt, iu1, iv1);
   float4 top, bottom, out;
   top.x = TL.x * inv_fu + TR.x * fu;
   top.y = TL.y * inv_fu + TR.y * fu;
@@ -163,11 +281,11 @@ __device__ __forceinline__ float4 vgx_sample(const VgxDraw &D, u32 slot, float u
     float f = lod - (float)l0;
     int l1 = l0 + 1 < (int)t.mips ? l0 + 1 : l0;
     u32 w0 = max(t.width >> l0, 1u), h0 = max(t.height >> l0, 1u);
-    float4 c0 = vgx_bilinear(base + t.mip_offset[l0], w0, h0, u, v);
+    float4 c0 = vgx_bilinear(base + t.mip_offset[l0], w0, h0, t.format, u, v);
     if(f > 0.0f)
     {
       u32 w1 = max(t.width >> l1, 1u), h1 = max(t.height >> l1, 1u);
-      float4 c1 = vgx_bilinear(base + t.mip_offset[l1], w1, h1, u, v);
+      float4 c1 = vgx_bilinear(base + t.mip_offset[l1], w1, h1, t.format, u, v);
       float g = 1.0f - f;
       c0.x = c0.x * g + c1.x * f;
       c0.y = c0.y * g + c1.y * f;
@@ -188,9 +306,38 @@ __device__ __forceinline__ float4 vgx_sample(const VgxDraw &D, u32 slot, float u
       iv -= t.height;
     iu = min(max(iu, 0), (int)t.width - 1);
     iv = min(max(iv, 0), (int)t.height - 1);
-    return vgx_texel(base, t.width, iu, iv);
+    return vgx_texel(base, t.width, t.format, iu, iv);
   }
-  return vgx_bilinear(base, t.width, t.height, u, v);
+  return vgx_bilinear(base, t.width, t.height, t.format, u, v);
+}
+
+/*
+ * sample_cube_wrapped (texture_sampling.cpp:186-250): the major axis picks the
+ * face, tested in this order so that a later match replaces an earlier one on
+ * ties; then the reference's bilinear sample of that face's mip 0 at
+ * 0.5 * (u / axis + 1).  The sampler object is ignored, as in the reference.
+ */
+__device__ __forceinline__ float4 vgx_sample_cube(const VgxDraw &D, u32 slot, float x, float y,
+                                                  float z)
+{
+  if(slot >= VGX_MAX_TEX || D.tex[slot].base == 0)
+    return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const VgxTex &t = D.tex[slot];
+  const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+  const bool px = x > 0.0f, py = y > 0.0f, pz = z > 0.0f;
+  float axis = 0.0f, u = 0.0f, v = 0.0f;
+  u32 face = 0;
+  if(px && ax >= ay && ax >= az) { axis = ax; u = -z; v = -y; face = 0; }
+  if(!px && ax >= ay && ax >= az) { axis = ax; u = z; v = -y; face = 1; }
+  if(py && ay >= ax && ay >= az) { axis = ay; u = x; v = z; face = 2; }
+  if(!py && ay >= ax && ay >= az) { axis = ay; u = x; v = -z; face = 3; }
+  if(pz && az >= ax && az >= ay) { axis = az; u = x; v = -y; face = 4; }
+  if(!pz && az >= ax && az >= ay) { axis = az; u = -x; v = -y; face = 5; }
+  if(face >= t.layers)
+    face = 0;
+  const u8 *base = (const u8 *)t.base + t.layer_bytes * face;
+  return vgx_bilinear(base, t.width, t.height, t.format, 0.5f * (u / axis + 1.0f),
+                      0.5f * (v / axis + 1.0f));
 }
 
 /* Four-lane CreateDot (spirv_compile.cpp:629-643) of the barycentrics with

@@ -132,16 +132,23 @@ __device__ __forceinline__ bool vgx_tri_indices(const VgxDraw &D, u32 local, u32
 
 extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
 {
+  __shared__ u32 s_draw;
+  const VgxDraw *draws = (const VgxDraw *)job.draws;
   vgx_init_unorm8();
+  /* the block's triangles are consecutive: one search for the first one's draw,
+     then each thread steps forward over the (few) draws the block spans */
+  if(threadIdx.x == 0)
+    s_draw = vgx_find_draw(draws, job.num_draws, min(blockIdx.x * blockDim.x, job.num_tris - 1));
   __syncthreads();
   const u32 tri = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = tri < job.num_tris;
-  const VgxDraw *draws = (const VgxDraw *)job.draws;
   u32 *counts = (u32 *)job.counts;
   u32 keep = 0, tested = 0;
   if(live)
   {
-    const u32 di = vgx_find_draw(draws, job.num_draws, tri);
+    u32 di = s_draw;
+    while(di + 1 < job.num_draws && draws[di + 1].tri_base <= tri)
+      di++;
     const VgxDraw &D = draws[di];
     const VgxTarget T = ((const VgxTarget *)job.targets)[D.target];
     const u32 local = tri - D.tri_base;

@@ -70,10 +70,18 @@ typedef struct VgxAttr {
   u32 stride;
 } VgxAttr;
 
+/* texel storage (VgxTex::format) */
+#define VGX_TEX_RGBA8 0u
+#define VGX_TEX_BC2 1u /* 16-byte 4x4 blocks: explicit 4-bit alpha + RGB565 palette */
+#define VGX_TEX_BC3 2u /* 16-byte 4x4 blocks: interpolated alpha + RGB565 palette */
+
 typedef struct VgxTex {
   u64 base; /* device address of mip 0 */
   u32 width, height, mips, filter;
   u32 mip_offset[VGX_MAX_MIPS + 1]; /* byte offset of each mip from base (tight packing) */
+  u32 format;                       /* VGX_TEX_* */
+  u32 layers;                       /* 6 for a cube map */
+  u64 layer_bytes;                  /* stride between layers (all mips of one layer) */
 } VgxTex;
 
 typedef struct VgxDraw {

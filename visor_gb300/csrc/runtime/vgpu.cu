@@ -234,11 +234,18 @@ __global__ void k_emit(VgxJob job, u32 rec_words, const u32 *offsets)
   const u32 total = offsets[job.num_tris];
   if(total > job.pair_capacity)
     return;
-  const int *r = (const int *)((const u32 *)job.records + (u64)tri * rec_words);
+  /* records start on 16-byte boundaries (whole uint4 words) */
+  const uint4 *r = (const uint4 *)((const u32 *)job.records + (u64)tri * rec_words);
   int head[VGX_REC_HEAD];
 #pragma unroll
-  for(int i = 0; i < VGX_REC_HEAD; i++)
-    head[i] = r[i];
+  for(int i = 0; i < VGX_REC_HEAD / 4; i++)
+  {
+    const uint4 v = __ldg(r + i);
+    head[4 * i] = (int)v.x;
+    head[4 * i + 1] = (int)v.y;
+    head[4 * i + 2] = (int)v.z;
+    head[4 * i + 3] = (int)v.w;
+  }
   const VgxDraw *draws = (const VgxDraw *)job.draws;
   const VgxTarget *targets = (const VgxTarget *)job.targets;
   const VgxTarget &T = targets[draws[head[R_DRAW]].target];
@@ -600,9 +607,11 @@ static int compile_cubin(const std::string &src, std::vector<char> &cubin, char 
 }
 
 static std::string full_source(const char *shader_source, uint32_t tile_shift, uint32_t warps = 1,
-                               uint32_t deferred = 0)
+                               uint32_t deferred = 0, uint32_t blocks = 0)
 {
   std::string src;
+  /* block-compressed texel decoding only where a job binds such a texture */
+  src += "#define VGX_TEX_BLOCKS " + std::to_string(blocks ? 1 : 0) + "\n";
   src += "#define VGX_TILE_SHIFT " + std::to_string(tile_shift) + "\n";
   src += "#define VGX_RASTER_WARPS " + std::to_string(warps) + "\n";
   src += "#define VGX_DEFERRED " + std::to_string(std::min<uint32_t>(deferred, 2)) + "\n";
@@ -618,9 +627,10 @@ extern "C" int vgpu_program_check(const char *shader_source, uint32_t tile_shift
                                   size_t log_size, uint64_t *cubin_bytes)
 {
   std::vector<char> cubin;
-  /* tile_shift carries the warps per bin in bits 8..15 and the shading mode in bits 16..17 */
+  /* tile_shift carries the warps per bin in bits 8..15, the shading mode in bits 16..17 and
+     block-compressed texture support in bit 18 */
   int rc = compile_cubin(full_source(shader_source, tile_shift & 0xff, std::max(1u, (tile_shift >> 8) & 0xff),
-                                     (tile_shift >> 16) & 3),
+                                     (tile_shift >> 16) & 3, (tile_shift >> 18) & 1),
                          cubin, log, log_size);
   if(cubin_bytes)
     *cubin_bytes = cubin.size();
@@ -678,20 +688,21 @@ static int load_cubin(const std::string &src, std::vector<char> &cubin, char *lo
 /* The variant of a program for a bin tile edge of 2^tile_shift pixels and
    `warps` warps per bin; compiled with NVRTC on first use. */
 static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, u32 deferred,
-                                int *rc_out)
+                                int *rc_out, u32 blocks = 0)
 {
   tile_shift = std::min<u32>(std::max<u32>(tile_shift, 3), 6);
   const u32 subs = 1u << (2 * (tile_shift - 3));
   warps = std::max<u32>(1, std::min<u32>(warps, std::min<u32>(subs, 16)));
   deferred = std::min<u32>(deferred, 2);
-  const u32 key = deferred << 16 | tile_shift << 8 | warps;
+  blocks = blocks ? 1 : 0;
+  const u32 key = blocks << 18 | deferred << 16 | tile_shift << 8 | warps;
   std::lock_guard<std::mutex> lk(p->mu);
   auto it = p->variants.find(key);
   if(it != p->variants.end())
     return it->second;
   std::vector<char> cubin;
   char log[4096] = {0};
-  int rc = load_cubin(full_source(p->source.c_str(), tile_shift, warps, deferred), cubin, log,
+  int rc = load_cubin(full_source(p->source.c_str(), tile_shift, warps, deferred, blocks), cubin, log,
                       sizeof(log));
   if(rc)
   {
@@ -1084,17 +1095,26 @@ static int list_build(vgpu_list *l)
   u64 rec_words = 0, cnt_words = 0;
   for(Job &j : l->jobs)
   {
+    /* no draw blends: the raster variant that shades each pixel's last fragment once;
+       with more triangles than pixels, records drop the interpolants (recomputed for
+       the shaded fragments) */
+    u32 mode = 0;
     if(j.all_opaque && j.num_tris)
     {
-      /* no draw blends: the raster variant that shades each pixel's last fragment once;
-         with more triangles than pixels, records drop the interpolants (recomputed for
-         the shaded fragments) */
       u64 pixels = 0;
       for(const VgxTarget &t : j.targets)
         pixels += (u64)t.width * (u32)t.height;
-      const u32 mode = (u64)j.num_tris > pixels ? 2u : 1u;
+      mode = (u64)j.num_tris > pixels ? 2u : 1u;
+    }
+    u32 blocks = 0;
+    for(const VgxDraw &d : j.draws)
+      for(int k = 0; k < VGX_MAX_TEX; k++)
+        if(d.tex[k].base && d.tex[k].format != VGX_TEX_RGBA8)
+          blocks = 1;
+    if(mode || blocks)
+    {
       int vrc = VGPU_OK;
-      VgpuVariant *dv = get_variant(j.prog, j.var->tile_shift, j.var->warps, mode, &vrc);
+      VgpuVariant *dv = get_variant(j.prog, j.var->tile_shift, j.var->warps, mode, &vrc, blocks);
       if(!dv)
         return vrc;
       j.var = dv;

@@ -230,7 +230,7 @@ static int fill_memory(vsd_context *c, Alloc *a, const void *src, VkDeviceSize b
 
 static int make_image(vsd_context *c, uint32_t w, uint32_t h, uint32_t mips, VkFormat fmt,
                       VkImageUsageFlags usage, uint32_t type, VkImageAspectFlags aspect,
-                      VkImage *img, Alloc *a, VkImageView *view)
+                      VkImage *img, Alloc *a, VkImageView *view, uint32_t layers = 1)
 {
   Fns &f = c->fn;
   VkImageCreateInfo ici = {};
@@ -241,7 +241,9 @@ static int make_image(vsd_context *c, uint32_t w, uint32_t h, uint32_t mips, VkF
   ici.extent.height = h;
   ici.extent.depth = 1;
   ici.mipLevels = mips;
-  ici.arrayLayers = 1;
+  ici.arrayLayers = layers;
+  if(layers == 6)
+    ici.flags = VK_IMAGE_CREATE_CUBE_COMPATIBLE_BIT;
   ici.samples = VK_SAMPLE_COUNT_1_BIT;
   ici.tiling = type == c->type_host ? VK_IMAGE_TILING_LINEAR : VK_IMAGE_TILING_OPTIMAL;
   ici.usage = usage;
@@ -259,11 +261,11 @@ static int make_image(vsd_context *c, uint32_t w, uint32_t h, uint32_t mips, VkF
   VkImageViewCreateInfo vci = {};
   vci.sType = VK_STRUCTURE_TYPE_IMAGE_VIEW_CREATE_INFO;
   vci.image = *img;
-  vci.viewType = VK_IMAGE_VIEW_TYPE_2D;
+  vci.viewType = layers == 6 ? VK_IMAGE_VIEW_TYPE_CUBE : VK_IMAGE_VIEW_TYPE_2D;
   vci.format = fmt;
   vci.subresourceRange.aspectMask = aspect;
   vci.subresourceRange.levelCount = mips;
-  vci.subresourceRange.layerCount = 1;
+  vci.subresourceRange.layerCount = layers;
   VSD_CHECK(f.vkCreateImageView(c->device, &vci, nullptr, view));
   return 0;
 }
@@ -546,9 +548,12 @@ extern "C" int vsd_upload(vsd_context *c, const vsc_scene *sc, uint32_t flags, v
   {
     const vsc_texture &tx = sc->textures[t];
     TextureObjs &o = s->textures[t];
-    TRY(make_image(c, tx.width, tx.height, tx.mips, VK_FORMAT_R8G8B8A8_UNORM,
+    const VkFormat fmt = tx.format == VSC_TEXFMT_BC2   ? VK_FORMAT_BC2_UNORM_BLOCK
+                         : tx.format == VSC_TEXFMT_BC3 ? VK_FORMAT_BC3_UNORM_BLOCK
+                                                       : VK_FORMAT_R8G8B8A8_UNORM;
+    TRY(make_image(c, tx.width, tx.height, tx.mips, fmt,
                    VK_IMAGE_USAGE_SAMPLED_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT, c->type_device,
-                   VK_IMAGE_ASPECT_COLOR_BIT, &o.image, &o.mem, &o.view));
+                   VK_IMAGE_ASPECT_COLOR_BIT, &o.image, &o.mem, &o.view, tx.layers ? tx.layers : 1));
     TRY(make_buffer(c, tx.bytes, VK_BUFFER_USAGE_TRANSFER_SRC_BIT, c->type_host, &o.staging,
                     &o.staging_mem));
     TRY(fill_memory(c, &o.staging_mem, tx.texels, tx.bytes));
@@ -669,12 +674,14 @@ extern "C" int vsd_upload(vsd_context *c, const vsc_scene *sc, uint32_t flags, v
   for(uint32_t t = 0; t < sc->num_textures; t++)
   {
     const vsc_texture &tx = sc->textures[t];
+    for(uint32_t l = 0; l < (tx.layers ? tx.layers : 1); l++)
     for(uint32_t m = 0; m < tx.mips; m++)
     {
       VkBufferImageCopy r = {};
-      r.bufferOffset = vsc_texture_mip_offset(&tx, m);
+      r.bufferOffset = vsc_texture_layer_bytes(&tx) * l + vsc_texture_mip_offset(&tx, m);
       r.imageSubresource.aspectMask = VK_IMAGE_ASPECT_COLOR_BIT;
       r.imageSubresource.mipLevel = m;
+      r.imageSubresource.baseArrayLayer = l;
       r.imageSubresource.layerCount = 1;
       r.imageExtent.width = (tx.width >> m) ? (tx.width >> m) : 1;
       r.imageExtent.height = (tx.height >> m) ? (tx.height >> m) : 1;

@@ -201,21 +201,26 @@ uint32_t vsc_add_pipeline(vsc_scene *s, const vsc_pipeline *p)
   return s->num_pipelines++;
 }
 
+uint32_t vsc_texture_bpp(uint32_t format) { return format == VSC_TEXFMT_RGBA8 ? 4u : 1u; }
+
 uint64_t vsc_texture_mip_offset(const vsc_texture *t, uint32_t mip)
 {
   /* tight per-mip packing, as CalcSubresourceByteOffset (precompiled.cpp:3-36) lays out layer 0 */
+  const uint32_t bpp = vsc_texture_bpp(t->format);
   uint64_t offs = 0;
   for(uint32_t m = 0; m < mip; m++)
   {
     uint32_t mw = t->width >> m, mh = t->height >> m;
     if(mw < 1) mw = 1;
     if(mh < 1) mh = 1;
-    offs += (uint64_t)mw * mh * 4;
+    offs += (uint64_t)mw * mh * bpp;
   }
   return offs;
 }
 
-static void build_mips(vsc_texture *t)
+uint64_t vsc_texture_layer_bytes(const vsc_texture *t) { return vsc_texture_mip_offset(t, t->mips); }
+
+static void build_mips_layer(vsc_texture *t, uint8_t *layer)
 {
   for(uint32_t m = 1; m < t->mips; m++)
   {
@@ -225,8 +230,8 @@ static void build_mips(vsc_texture *t)
     if(ph < 1) ph = 1;
     if(mw < 1) mw = 1;
     if(mh < 1) mh = 1;
-    const uint8_t *src = t->texels + vsc_texture_mip_offset(t, m - 1);
-    uint8_t *dst = t->texels + vsc_texture_mip_offset(t, m);
+    const uint8_t *src = layer + vsc_texture_mip_offset(t, m - 1);
+    uint8_t *dst = layer + vsc_texture_mip_offset(t, m);
     for(uint32_t y = 0; y < mh; y++)
       for(uint32_t x = 0; x < mw; x++)
       {
@@ -241,6 +246,8 @@ static void build_mips(vsc_texture *t)
       }
   }
 }
+
+static void build_mips(vsc_texture *t) { build_mips_layer(t, t->texels); }
 
 static uint32_t add_texture_id(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
                                const uint8_t *texels, uint64_t seed, uint64_t id);
@@ -262,6 +269,8 @@ static uint32_t add_texture_id(vsc_scene *s, uint32_t width, uint32_t height, ui
   t->width = width;
   t->height = height;
   t->mips = mips ? mips : 1;
+  t->format = VSC_TEXFMT_RGBA8;
+  t->layers = 1;
   t->bytes = vsc_texture_mip_offset(t, t->mips);
   t->texels = (uint8_t *)malloc((size_t)t->bytes);
   uint64_t mip0 = (uint64_t)width * height * 4;
@@ -279,6 +288,39 @@ static uint32_t add_texture_id(vsc_scene *s, uint32_t width, uint32_t height, ui
     }
   }
   build_mips(t);
+  return s->num_textures++;
+}
+
+uint32_t vsc_add_texture_fmt(vsc_scene *s, uint32_t width, uint32_t height, uint32_t mips,
+                             uint32_t format, uint32_t layers, uint64_t seed)
+{
+  uint64_t cap = s->cap_textures;
+  GROW(s->textures, cap, (uint64_t)s->num_textures + 1, vsc_texture);
+  s->cap_textures = (uint32_t)cap;
+  const uint64_t id = s->num_textures;
+  vsc_texture *t = &s->textures[id];
+  t->width = width;
+  t->height = height;
+  t->mips = mips ? mips : 1;
+  t->format = format;
+  t->layers = layers ? layers : 1;
+  const uint64_t slice = vsc_texture_layer_bytes(t);
+  t->bytes = slice * t->layers;
+  t->texels = (uint8_t *)malloc((size_t)t->bytes);
+  rng r = rng_for(seed, 0xfd, id);
+  for(uint32_t l = 0; l < t->layers; l++)
+  {
+    uint8_t *layer = t->texels + slice * l;
+    /* RGBA8: random mip 0, box-filtered mips; block formats: random blocks at every level */
+    const uint64_t n = format == VSC_TEXFMT_RGBA8 ? (uint64_t)width * height * 4 : slice;
+    for(uint64_t i = 0; i < n; i += 4)
+    {
+      uint32_t v = urand_u32(&r);
+      memcpy(layer + i, &v, n - i < 4 ? (size_t)(n - i) : 4);
+    }
+    if(format == VSC_TEXFMT_RGBA8)
+      build_mips_layer(t, layer);
+  }
   return s->num_textures++;
 }
 
@@ -343,7 +385,8 @@ uint32_t vsc_stride_of(uint32_t shader)
 {
   switch(shader)
   {
-    case VSC_SHADER_LAMBERT_TEX: return VSC_STRIDE_LAMBERT_TEX;
+    case VSC_SHADER_LAMBERT_TEX:
+    case VSC_SHADER_CUBE: return VSC_STRIDE_LAMBERT_TEX;
     case VSC_SHADER_COLOR: return VSC_STRIDE_COLOR;
     case VSC_SHADER_LAMBERT_TEX_ALPHA: return VSC_STRIDE_LAMBERT_TEX_ALPHA;
     default: return 0;
@@ -356,10 +399,11 @@ uint32_t vsc_vertex_attrs(uint32_t shader, vsc_attr *a)
   {
     case VSC_SHADER_LAMBERT_TEX:
     case VSC_SHADER_LAMBERT_TEX_ALPHA:
+    case VSC_SHADER_CUBE:
       a[0].location = 0; a[0].format = 106; a[0].offset = 0;  /* position */
       a[1].location = 1; a[1].format = 106; a[1].offset = 12; /* normal */
       a[2].location = 2; a[2].format = 103; a[2].offset = 24; /* uv */
-      if(shader == VSC_SHADER_LAMBERT_TEX)
+      if(shader != VSC_SHADER_LAMBERT_TEX_ALPHA)
         return 3;
       a[3].location = 3; a[3].format = 100; a[3].offset = 32; /* alpha */
       return 4;

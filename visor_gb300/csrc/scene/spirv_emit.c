@@ -431,6 +431,38 @@ static size_t emit_color_fs(uint32_t *words, size_t cap)
   return finish(&m, &c, 4, "visor_shader:color.frag", iface, 2, 1, words, cap);
 }
 
+/* samplerCube at binding 0, read at the interpolated (unnormalised) normal */
+static size_t emit_cube_fs(uint32_t *words, size_t cap)
+{
+  mod m;
+  common c;
+  begin(&m, &c);
+  uint32_t img = m.next++;
+  I(&m.types, OpTypeImage, img, c.tfloat, 3 /* Cube */, 0, 0, 0, 1, 0 /* Unknown */);
+  uint32_t simg = m.next++;
+  I(&m.types, OpTypeSampledImage, simg, img);
+  uint32_t puc = ptr(&m, SCUniformConstant, simg);
+  uint32_t tex = var(&m, puc, SCUniformConstant);
+  I(&m.annot, OpDecorate, tex, DecDescriptorSet, 0);
+  I(&m.annot, OpDecorate, tex, DecBinding, 0);
+  uint32_t pin3 = ptr(&m, SCInput, c.vec3), pout4 = ptr(&m, SCOutput, c.vec4);
+  uint32_t inNrm = var(&m, pin3, SCInput), outCol = var(&m, pout4, SCOutput);
+  decorate_loc(&m, inNrm, 0);
+  decorate_loc(&m, outCol, 0);
+  buf *f = &m.code;
+  I(f, OpFunction, c.tvoid, c.main, 0, c.tfn);
+  I(f, OpLabel, m.next++);
+  uint32_t n = m.next++, smp = m.next++, t = m.next++;
+  I(f, OpLoad, c.vec3, n, inNrm);
+  I(f, OpLoad, simg, smp, tex);
+  I(f, OpImageSampleImplicitLod, c.vec4, t, smp, n);
+  I(f, OpStore, outCol, t);
+  inst(f, OpReturn, 0, NULL);
+  inst(f, OpFunctionEnd, 0, NULL);
+  uint32_t iface[2] = {inNrm, outCol};
+  return finish(&m, &c, 4, "visor_shader:cube.frag", iface, 2, 1, words, cap);
+}
+
 size_t vspv_emit(uint32_t shader, uint32_t stage, uint32_t *words, size_t capacity)
 {
   switch(shader)
@@ -444,6 +476,9 @@ size_t vspv_emit(uint32_t shader, uint32_t stage, uint32_t *words, size_t capaci
     case VSC_SHADER_COLOR:
       return stage == VSPV_STAGE_VERTEX ? emit_color_vs(words, capacity)
                                         : emit_color_fs(words, capacity);
+    case VSC_SHADER_CUBE:
+      return stage == VSPV_STAGE_VERTEX ? emit_lambert_vs(0, words, capacity)
+                                        : emit_cube_fs(words, capacity);
     default: return 0;
   }
 }

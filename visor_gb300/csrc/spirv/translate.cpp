@@ -1110,8 +1110,12 @@ bool Gen::emit_inst(std::ostringstream &o, const Inst &in, const Func &f,
       const Type &it = T(m.rtype.at(img));
       if(it.dim == 3)
       {
-        err = "cube-map sampling is not supported on the GPU path";
-        return false;
+        /* sample_cube_wrapped (texture_sampling.cpp:186-250): face from the major axis */
+        o << ind << "{ float4 t_ = vgx_sample_cube(*ctx.D, (u32)(" << val(img) << "), "
+          << comp(coord, 0) << ", " << comp(coord, 1) << ", " << comp(coord, 2) << "); v" << id()
+          << "[0] = t_.x; v" << id() << "[1] = t_.y; v" << id() << "[2] = t_.z; v" << id()
+          << "[3] = t_.w; }\n";
+        return true;
       }
       o << ind << "{ float4 t_ = vgx_sample(*ctx.D, (u32)(" << val(img) << "), " << comp(coord, 0)
         << ", " << comp(coord, 1) << ", " << lod << "); v" << id() << "[0] = t_.x; v" << id()

@@ -11,6 +11,9 @@ import numpy as np
 SHADER_LAMBERT_TEX = 1
 SHADER_COLOR = 2
 SHADER_LAMBERT_TEX_ALPHA = 3
+SHADER_CUBE = 4
+
+TEXFMT_RGBA8, TEXFMT_BC2, TEXFMT_BC3 = 0, 1, 2
 
 FILTER_REFERENCE = 0
 FILTER_TRILINEAR = 1
@@ -40,7 +43,8 @@ class Pipeline(C.Structure):
 
 class Texture(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("mips", C.c_uint32),
-                ("bytes", C.c_uint64), ("texels", C.POINTER(C.c_uint8))]
+                ("bytes", C.c_uint64), ("texels", C.POINTER(C.c_uint8)), ("format", C.c_uint32),
+                ("layers", C.c_uint32)]
 
 
 class Target(C.Structure):
@@ -96,6 +100,9 @@ def bind_scene_api(lib):
     lib.vsc_add_pipeline.restype = C.c_uint32
     lib.vsc_add_texture.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64]
     lib.vsc_add_texture.restype = C.c_uint32
+    lib.vsc_add_texture_fmt.argtypes = [SP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                        C.c_uint64]
+    lib.vsc_add_texture_fmt.restype = C.c_uint32
     lib.vsc_add_vertices.argtypes = [SP, C.c_void_p, C.c_uint64]
     lib.vsc_add_vertices.restype = C.c_uint64
     lib.vsc_add_indices.argtypes = [SP, C.c_void_p, C.c_uint64]
