@@ -77,6 +77,8 @@ void vgpu_list_clear(vgpu_list *l, const VgxTarget *target, int color, int depth
 /* one draw; consecutive draws with the same program may be merged into one job */
 void vgpu_list_draw(vgpu_list *l, vgpu_program *prog, const VgxDraw *draw, const VgxTarget *target);
 /* host-visible memory refresh before (upload) and after (download) the list */
+/* An image blit between RGBA8 subresources (ends a segment, like a copy). */
+void vgpu_list_blit(vgpu_list *l, const VgxBlit *blit);
 void vgpu_list_upload(vgpu_list *l, void *dev, const void *host, uint64_t bytes);
 void vgpu_list_download(vgpu_list *l, void *host, const void *dev, uint64_t bytes);
 

@@ -180,7 +180,7 @@ struct VkCommandPool_T
 enum class Pkt : uint16_t
 {
   BeginRP, EndRP, BindPipeline, BindSet, BindVB, BindIB, SetViewport, SetScissor, Push, Draw,
-  DrawIndexed, CopyBuf2Img, CopyBuf, Barrier
+  DrawIndexed, CopyBuf2Img, CopyBuf, Barrier, Blit
 };
 
 struct VkCommandBuffer_T
@@ -1075,6 +1075,12 @@ struct CopyBuf
   VkBuffer src, dst;
   VkBufferCopy region;
 };
+struct Blit
+{
+  VkImage src, dst;
+  VkImageBlit region;
+  VkFilter filter;
+};
 struct Viewport
 {
   VkViewport v;
@@ -1171,6 +1177,18 @@ VISOR_EXPORT void vkCmdCopyBufferToImage(VkCommandBuffer c, VkBuffer src, VkImag
   {
     pk::CopyBuf2Img b = {src, dst, regions[i]};
     c->push(Pkt::CopyBuf2Img, b);
+  }
+}
+
+/* No counterpart in the reference (its tables have no vkCmdBlitImage): RGBA8 blits
+   between subresources, used to build mip chains on the GPU. */
+VISOR_EXPORT void vkCmdBlitImage(VkCommandBuffer c, VkImage src, VkImageLayout, VkImage dst, VkImageLayout,
+                                 uint32_t n, const VkImageBlit *regions, VkFilter filter)
+{
+  for(uint32_t i = 0; i < n; i++)
+  {
+    pk::Blit b = {src, dst, regions[i], filter};
+    c->push(Pkt::Blit, b);
   }
 }
 
@@ -1492,6 +1510,42 @@ void lower(VkCommandBuffer c)
         }
         break;
       }
+      case Pkt::Blit:
+      {
+        pk::Blit b;
+        pull(&b, sizeof(b));
+        VkImage_T *si = b.src, *di = b.dst;
+        const VkImageBlit &r = b.region;
+        if(!si->mem || !di->mem || si->bpp != 4 || di->bpp != 4)
+          break; /* RGBA8 only */
+        const uint32_t sm = r.srcSubresource.mipLevel, dm = r.dstSubresource.mipLevel;
+        const uint32_t layers = std::max(1u, r.srcSubresource.layerCount);
+        for(uint32_t ly = 0; ly < layers; ly++)
+        {
+          VgxBlit bl;
+          memset(&bl, 0, sizeof(bl));
+          bl.src = (u64)dev_addr(si->mem, si->offset + subresource_offset(si, sm, r.srcSubresource.baseArrayLayer + ly));
+          bl.dst = (u64)dev_addr(di->mem, di->offset + subresource_offset(di, dm, r.dstSubresource.baseArrayLayer + ly));
+          bl.src_w = std::max(1u, si->extent.width >> sm);
+          bl.src_h = std::max(1u, si->extent.height >> sm);
+          bl.dst_w = std::max(1u, di->extent.width >> dm);
+          bl.dst_h = std::max(1u, di->extent.height >> dm);
+          bl.sx0 = std::min(r.srcOffsets[0].x, r.srcOffsets[1].x);
+          bl.sx1 = std::max(r.srcOffsets[0].x, r.srcOffsets[1].x);
+          bl.sy0 = std::min(r.srcOffsets[0].y, r.srcOffsets[1].y);
+          bl.sy1 = std::max(r.srcOffsets[0].y, r.srcOffsets[1].y);
+          bl.dx0 = std::min(r.dstOffsets[0].x, r.dstOffsets[1].x);
+          bl.dx1 = std::max(r.dstOffsets[0].x, r.dstOffsets[1].x);
+          bl.dy0 = std::min(r.dstOffsets[0].y, r.dstOffsets[1].y);
+          bl.dy1 = std::max(r.dstOffsets[0].y, r.dstOffsets[1].y);
+          bl.filter = b.filter == VK_FILTER_LINEAR ? 1u : 0u;
+          vgpu_list_blit(l, &bl);
+        }
+        note_read(use, si->mem);
+        note_read(use, di->mem); /* parts outside the rectangle keep their bytes */
+        note_write(use, di->mem);
+        break;
+      }
       case Pkt::CopyBuf:
       {
         pk::CopyBuf b;
@@ -1590,6 +1644,7 @@ const Entry kDeviceFns[] = {
     ICD_ENTRY(vkCmdBindDescriptorSets), ICD_ENTRY(vkCmdSetViewport), ICD_ENTRY(vkCmdSetScissor),
     ICD_ENTRY(vkCmdPushConstants), ICD_ENTRY(vkCmdDraw), ICD_ENTRY(vkCmdDrawIndexed),
     ICD_ENTRY(vkCmdCopyBufferToImage), ICD_ENTRY(vkCmdCopyBuffer), ICD_ENTRY(vkQueueSubmit),
+    ICD_ENTRY(vkCmdBlitImage),
     ICD_ENTRY(vkWaitForFences), ICD_ENTRY(vkResetFences), ICD_ENTRY(vkDeviceWaitIdle), ICD_ENTRY(vkQueueWaitIdle),
 };
 

@@ -114,6 +114,17 @@ typedef struct VgxTarget {
   float clear_depth;
 } VgxTarget;
 
+/* One RGBA8 image-to-image blit (vkCmdBlitImage): rectangles [x0, x1) x [y0, y1)
+   of a source and a destination subresource. */
+typedef struct VgxBlit {
+  u64 src, dst;            /* device addresses of the two subresources */
+  u32 src_w, src_h, dst_w, dst_h; /* subresource sizes in texels */
+  i32 sx0, sy0, sx1, sy1;  /* source rectangle */
+  i32 dx0, dy0, dx1, dy1;  /* destination rectangle */
+  u32 filter;              /* 0 nearest, 1 linear */
+  u32 reserved;
+} VgxBlit;
+
 typedef struct VgxJob {
   u64 draws;   /* VgxDraw* */
   u64 targets; /* VgxTarget* */

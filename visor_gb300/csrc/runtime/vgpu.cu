@@ -431,6 +431,80 @@ __global__ void k_clear(VgxTarget t, int color, int depth)
   }
 }
 
+/*
+ * vkCmdBlitImage of RGBA8 subresources.  An exactly 2:1 linear blit (mip
+ * generation) averages the 2x2 source texels per channel with rounding half up,
+ * (a + b + c + d + 2) >> 2.  Other blits sample at the destination texel centre
+ * mapped into the source rectangle, clamped to the source image: nearest takes
+ * that texel, linear interpolates the four around it and rounds to nearest.
+ */
+__global__ void k_blit(VgxBlit b)
+{
+  const int dw = b.dx1 - b.dx0, dh = b.dy1 - b.dy0;
+  const int sw = b.sx1 - b.sx0, sh = b.sy1 - b.sy0;
+  if(dw <= 0 || dh <= 0 || sw <= 0 || sh <= 0)
+    return;
+  const u32 *src = (const u32 *)b.src;
+  u32 *dst = (u32 *)b.dst;
+  const bool box = b.filter == 1u && sw == 2 * dw && sh == 2 * dh;
+  const float scx = (float)sw / (float)dw, scy = (float)sh / (float)dh;
+  const u64 n = (u64)dw * (u32)dh;
+  for(u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)
+  {
+    const int ox = (int)(i % (u32)dw), oy = (int)(i / (u32)dw);
+    const int x = b.dx0 + ox, y = b.dy0 + oy;
+    if(x < 0 || y < 0 || x >= (int)b.dst_w || y >= (int)b.dst_h)
+      continue;
+    u32 out = 0;
+    if(box)
+    {
+      const int sx = min(max(b.sx0 + 2 * ox, 0), (int)b.src_w - 1);
+      const int sy = min(max(b.sy0 + 2 * oy, 0), (int)b.src_h - 1);
+      const int sx1 = min(sx + 1, (int)b.src_w - 1), sy1 = min(sy + 1, (int)b.src_h - 1);
+      const u32 t[4] = {src[(u64)sy * b.src_w + sx], src[(u64)sy * b.src_w + sx1],
+                        src[(u64)sy1 * b.src_w + sx], src[(u64)sy1 * b.src_w + sx1]};
+#pragma unroll
+      for(int c = 0; c < 4; c++)
+      {
+        const u32 sum = ((t[0] >> (8 * c)) & 255u) + ((t[1] >> (8 * c)) & 255u) +
+                        ((t[2] >> (8 * c)) & 255u) + ((t[3] >> (8 * c)) & 255u);
+        out |= ((sum + 2u) >> 2) << (8 * c);
+      }
+    }
+    else
+    {
+      const float u = (float)b.sx0 + ((float)ox + 0.5f) * scx;
+      const float v = (float)b.sy0 + ((float)oy + 0.5f) * scy;
+      if(b.filter != 1u)
+      {
+        const int sx = min(max((int)floorf(u), 0), (int)b.src_w - 1);
+        const int sy = min(max((int)floorf(v), 0), (int)b.src_h - 1);
+        out = src[(u64)sy * b.src_w + sx];
+      }
+      else
+      {
+        const float fu = u - 0.5f, fv = v - 0.5f;
+        const int x0 = (int)floorf(fu), y0 = (int)floorf(fv);
+        const float ax = fu - (float)x0, ay = fv - (float)y0;
+        const int cx0 = min(max(x0, 0), (int)b.src_w - 1), cx1 = min(max(x0 + 1, 0), (int)b.src_w - 1);
+        const int cy0 = min(max(y0, 0), (int)b.src_h - 1), cy1 = min(max(y0 + 1, 0), (int)b.src_h - 1);
+        const u32 t00 = src[(u64)cy0 * b.src_w + cx0], t10 = src[(u64)cy0 * b.src_w + cx1];
+        const u32 t01 = src[(u64)cy1 * b.src_w + cx0], t11 = src[(u64)cy1 * b.src_w + cx1];
+#pragma unroll
+        for(int c = 0; c < 4; c++)
+        {
+          const float a00 = (float)((t00 >> (8 * c)) & 255u), a10 = (float)((t10 >> (8 * c)) & 255u);
+          const float a01 = (float)((t01 >> (8 * c)) & 255u), a11 = (float)((t11 >> (8 * c)) & 255u);
+          const float top = a00 * (1.0f - ax) + a10 * ax, bot = a01 * (1.0f - ax) + a11 * ax;
+          const float val = top * (1.0f - ay) + bot * ay;
+          out |= (u32)min(max((int)floorf(val + 0.5f), 0), 255) << (8 * c);
+        }
+      }
+    }
+    dst[(u64)y * b.dst_w + x] = out;
+  }
+}
+
 __global__ void k_flag_overflow(const u32 *pair_total, u32 capacity, u32 *status)
 {
   if(*pair_total > capacity)
@@ -773,7 +847,7 @@ extern "C" uint32_t vgpu_program_record_words(const vgpu_program *p) { return p-
 
 namespace
 {
-enum CmdType { CMD_COPY, CMD_CLEAR, CMD_DRAW };
+enum CmdType { CMD_COPY, CMD_CLEAR, CMD_DRAW, CMD_BLIT };
 
 struct Cmd
 {
@@ -785,7 +859,22 @@ struct Cmd
   int color = 0, depth = 0;
   vgpu_program *prog = nullptr;
   VgxDraw draw;
+  VgxBlit blit;
 };
+
+/* a copy or blit command (they end a segment) on q's stream */
+static cudaError_t exec_copy(cudaStream_t stream, const Cmd &c, u64 *launches)
+{
+  if(c.type == CMD_BLIT)
+  {
+    const u64 n = (u64)std::max(0, c.blit.dx1 - c.blit.dx0) * (u64)std::max(0, c.blit.dy1 - c.blit.dy0);
+    const unsigned g = (unsigned)std::max<u64>(1, std::min<u64>((n + 255) / 256, (u64)g_sms * 16));
+    k_blit<<<g, 256, 0, stream>>>(c.blit);
+    (*launches)++;
+    return cudaGetLastError();
+  }
+  return cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, stream);
+}
 
 struct Job
 {
@@ -907,6 +996,15 @@ extern "C" void vgpu_list_copy(vgpu_list *l, void *dst, const void *src, uint64_
   l->built = false;
 }
 
+extern "C" void vgpu_list_blit(vgpu_list *l, const VgxBlit *b)
+{
+  Cmd c;
+  c.type = CMD_BLIT;
+  c.blit = *b;
+  l->cmds.push_back(c);
+  l->built = false;
+}
+
 extern "C" void vgpu_list_clear(vgpu_list *l, const VgxTarget *t, int color, int depth)
 {
   Cmd c;
@@ -982,7 +1080,7 @@ static int list_build(vgpu_list *l)
   for(size_t ci = 0; ci < l->cmds.size(); ci++)
   {
     Cmd &c = l->cmds[ci];
-    if(c.type == CMD_COPY)
+    if(c.type == CMD_COPY || c.type == CMD_BLIT)
     {
       close_job();
       flush_pending();
@@ -1576,7 +1674,7 @@ static int submit_plain(vgpu_queue *q, vgpu_list *l)
     if(e < l->plan.size() && l->plan[e].kind == Exec::E_COPY)
     {
       const Cmd &c = l->cmds[l->plan[e].index];
-      CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, q->stream));
+      CK(exec_copy(q->stream, c, &q->launches));
     }
     p = e + 1;
   }
@@ -1765,7 +1863,7 @@ static int capture_graph(vgpu_queue *q, vgpu_list *l)
     if(rc == VGPU_OK && e < l->plan.size() && l->plan[e].kind == Exec::E_COPY)
     {
       const Cmd &c = l->cmds[l->plan[e].index];
-      rec(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, q->stream));
+      rec(exec_copy(q->stream, c, &q->launches));
     }
     p = e + 1;
   }
@@ -2236,7 +2334,7 @@ extern "C" int vgpu_submit_noalloc(vgpu_queue *q, vgpu_list *l)
     if(e < l->plan.size() && l->plan[e].kind == Exec::E_COPY)
     {
       const Cmd &c = l->cmds[l->plan[e].index];
-      CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, q->stream));
+      CK(exec_copy(q->stream, c, &q->launches));
     }
     p = e + 1;
   }
@@ -2266,7 +2364,7 @@ extern "C" int vgpu_list_build_pooled(vgpu_list *l, void *pool, void *stream, ui
   l->ext_totals = h_totals;
   l->ext_totals_cap = h_totals_cap;
   for(const Cmd &c : l->cmds)
-    if(c.type == CMD_COPY)
+    if(c.type == CMD_COPY || c.type == CMD_BLIT)
       return VGPU_ERROR_INITIALIZATION_FAILED; /* copies would split the list into segments */
   return list_build(l);
 }

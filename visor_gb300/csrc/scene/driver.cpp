@@ -45,7 +45,7 @@ struct Fns
   X(vkAllocateCommandBuffers) X(vkFreeCommandBuffers) X(vkBeginCommandBuffer)                 \
   X(vkEndCommandBuffer) X(vkCmdBindPipeline) X(vkCmdBindDescriptorSets)                       \
   X(vkCmdBindIndexBuffer) X(vkCmdBindVertexBuffers) X(vkCmdDraw) X(vkCmdDrawIndexed)          \
-  X(vkCmdCopyBuffer) X(vkCmdCopyBufferToImage) X(vkCmdPushConstants)                          \
+  X(vkCmdCopyBuffer) X(vkCmdCopyBufferToImage) X(vkCmdBlitImage) X(vkCmdPushConstants)                          \
   X(vkCmdBeginRenderPass) X(vkCmdEndRenderPass)
   VSD_FNS(VSD_FN)
 #undef VSD_FN
@@ -674,8 +674,10 @@ extern "C" int vsd_upload(vsd_context *c, const vsc_scene *sc, uint32_t flags, v
   for(uint32_t t = 0; t < sc->num_textures; t++)
   {
     const vsc_texture &tx = sc->textures[t];
+    /* with VSD_GPU_MIPS an RGBA8 texture sends mip 0 and blits the rest on the device */
+    const bool gpu_mips = (flags & VSD_GPU_MIPS) && tx.format == VSC_TEXFMT_RGBA8 && tx.mips > 1;
     for(uint32_t l = 0; l < (tx.layers ? tx.layers : 1); l++)
-    for(uint32_t m = 0; m < tx.mips; m++)
+    for(uint32_t m = 0; m < (gpu_mips ? 1u : tx.mips); m++)
     {
       VkBufferImageCopy r = {};
       r.bufferOffset = vsc_texture_layer_bytes(&tx) * l + vsc_texture_mip_offset(&tx, m);
@@ -688,6 +690,23 @@ extern "C" int vsd_upload(vsd_context *c, const vsc_scene *sc, uint32_t flags, v
       r.imageExtent.depth = 1;
       f.vkCmdCopyBufferToImage(upload, s->textures[t].staging, s->textures[t].image,
                                VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &r);
+    }
+    for(uint32_t m = 1; gpu_mips && m < tx.mips; m++)
+    {
+      VkImageBlit b = {};
+      b.srcSubresource.aspectMask = b.dstSubresource.aspectMask = VK_IMAGE_ASPECT_COLOR_BIT;
+      b.srcSubresource.mipLevel = m - 1;
+      b.dstSubresource.mipLevel = m;
+      b.srcSubresource.layerCount = b.dstSubresource.layerCount = tx.layers ? tx.layers : 1;
+      b.srcOffsets[1].x = (int32_t)((tx.width >> (m - 1)) ? (tx.width >> (m - 1)) : 1);
+      b.srcOffsets[1].y = (int32_t)((tx.height >> (m - 1)) ? (tx.height >> (m - 1)) : 1);
+      b.srcOffsets[1].z = 1;
+      b.dstOffsets[1].x = (int32_t)((tx.width >> m) ? (tx.width >> m) : 1);
+      b.dstOffsets[1].y = (int32_t)((tx.height >> m) ? (tx.height >> m) : 1);
+      b.dstOffsets[1].z = 1;
+      f.vkCmdBlitImage(upload, s->textures[t].image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL,
+                       s->textures[t].image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &b,
+                       VK_FILTER_LINEAR);
     }
   }
   VSD_CHECK(f.vkEndCommandBuffer(upload));
