@@ -34,6 +34,8 @@ enum {
   VSD_RESTAGE_INPUTS = 1u << 0, /* re-copy vertex/index staging buffers into device memory every submit */
   VSD_DEVICE_TARGETS = 1u << 1, /* render targets in device-local memory (no readback) */
   VSD_GPU_MIPS = 1u << 2,       /* upload RGBA8 mip 0 only; build the chain with vkCmdBlitImage */
+  VSD_PRESENT = 1u << 3,        /* target 0's colour is a swapchain image of a headless surface,
+                                   presented after every submit and read back from the present */
 };
 
 /*

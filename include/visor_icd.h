@@ -36,6 +36,30 @@ PFN_vkVoidFunction vk_icdGetInstanceProcAddr(VkInstance instance, const char *pN
 PFN_vkVoidFunction vk_icdGetPhysicalDeviceProcAddr(VkInstance instance, const char *pName);
 PFN_vkVoidFunction vkGetDeviceProcAddr(VkDevice device, const char *pName);
 
+/*
+ * Presentation is headless (the reference presents with GDI, wsi.cpp).  Surfaces
+ * come from vkCreateHeadlessSurfaceEXT (VK_EXT_headless_surface, newer than the
+ * Vulkan header the reference vendors, so its create-info is declared here with
+ * the registry's layout); swapchains (VK_KHR_swapchain) keep their images in
+ * device memory and vkQueuePresentKHR copies the presented image to a pinned
+ * host copy in queue order.  With VISOR_GB300_PRESENT_DIR set, each present is
+ * also written there as frame_NNNNNN.ppm.
+ */
+#define VISOR_STRUCTURE_TYPE_HEADLESS_SURFACE_CREATE_INFO_EXT 1000256000
+typedef struct VisorHeadlessSurfaceCreateInfoEXT {
+  VkStructureType sType;
+  const void *pNext;
+  VkFlags flags;
+} VisorHeadlessSurfaceCreateInfoEXT;
+
+VkResult vkCreateHeadlessSurfaceEXT(VkInstance instance, const VisorHeadlessSurfaceCreateInfoEXT *info,
+                                    const VkAllocationCallbacks *allocator, VkSurfaceKHR *surface);
+typedef VkResult(VKAPI_PTR *PFN_vkCreateHeadlessSurfaceEXT_visor)(VkInstance, const VisorHeadlessSurfaceCreateInfoEXT *,
+                                                                  const VkAllocationCallbacks *, VkSurfaceKHR *);
+/* No counterpart in the reference: the last presented contents of swapchain image
+   `index` (BGRA8, width*height*4 bytes), once the queue has finished presenting. */
+VkResult visor_gb300_swapchain_read(VkSwapchainKHR swapchain, uint32_t index, void *dst, size_t size);
+
 /* Execution mode for command buffers lowered after this call: VGPU_MODE_BATCHED
    (default) or VGPU_MODE_PER_DRAW.  The environment variable VISOR_GB300_MODE
    ("batched" / "per_draw") sets the initial value. */

@@ -51,6 +51,8 @@ VK_DEFINE_HANDLE(VkDevice)
 VK_DEFINE_HANDLE(VkQueue)
 VK_DEFINE_HANDLE(VkCommandBuffer)
 VK_DEFINE_NON_DISPATCHABLE_HANDLE(VkSemaphore)
+VK_DEFINE_NON_DISPATCHABLE_HANDLE(VkSurfaceKHR)
+VK_DEFINE_NON_DISPATCHABLE_HANDLE(VkSwapchainKHR)
 VK_DEFINE_NON_DISPATCHABLE_HANDLE(VkFence)
 VK_DEFINE_NON_DISPATCHABLE_HANDLE(VkDeviceMemory)
 VK_DEFINE_NON_DISPATCHABLE_HANDLE(VkBuffer)
@@ -91,6 +93,9 @@ typedef enum VkResult {
   VK_ERROR_INCOMPATIBLE_DRIVER = -9,
   VK_ERROR_TOO_MANY_OBJECTS = -10,
   VK_ERROR_FORMAT_NOT_SUPPORTED = -11,
+  VK_ERROR_SURFACE_LOST_KHR = -1000000000,
+  VK_SUBOPTIMAL_KHR = 1000001003,
+  VK_ERROR_OUT_OF_DATE_KHR = -1000001004,
   VK_RESULT_MAX_ENUM = 0x7FFFFFFF
 } VkResult;
 
@@ -138,6 +143,8 @@ typedef enum VkStructureType {
   VK_STRUCTURE_TYPE_BUFFER_MEMORY_BARRIER = 44,
   VK_STRUCTURE_TYPE_IMAGE_MEMORY_BARRIER = 45,
   VK_STRUCTURE_TYPE_MEMORY_BARRIER = 46,
+  VK_STRUCTURE_TYPE_SWAPCHAIN_CREATE_INFO_KHR = 1000001000,
+  VK_STRUCTURE_TYPE_PRESENT_INFO_KHR = 1000001001,
   VK_STRUCTURE_TYPE_MAX_ENUM = 0x7FFFFFFF
 } VkStructureType;
 
@@ -208,6 +215,7 @@ typedef enum VkImageLayout {
   VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL = 6,
   VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL = 7,
   VK_IMAGE_LAYOUT_PREINITIALIZED = 8,
+  VK_IMAGE_LAYOUT_PRESENT_SRC_KHR = 1000001002,
   VK_IMAGE_LAYOUT_MAX_ENUM = 0x7FFFFFFF
 } VkImageLayout;
 
@@ -1536,6 +1544,90 @@ typedef void(VKAPI_PTR *PFN_vkCmdDrawIndexed)(VkCommandBuffer, uint32_t, uint32_
 typedef void(VKAPI_PTR *PFN_vkCmdCopyBuffer)(VkCommandBuffer, VkBuffer, VkBuffer, uint32_t, const VkBufferCopy *);
 typedef void(VKAPI_PTR *PFN_vkCmdCopyBufferToImage)(VkCommandBuffer, VkBuffer, VkImage, VkImageLayout, uint32_t, const VkBufferImageCopy *);
 typedef void(VKAPI_PTR *PFN_vkCmdBlitImage)(VkCommandBuffer, VkImage, VkImageLayout, VkImage, VkImageLayout, uint32_t, const VkImageBlit *, VkFilter);
+
+/* VK_KHR_surface / VK_KHR_swapchain (the reference implements these for Win32, wsi.cpp) */
+typedef enum VkColorSpaceKHR {
+  VK_COLOR_SPACE_SRGB_NONLINEAR_KHR = 0
+} VkColorSpaceKHR;
+
+typedef enum VkPresentModeKHR {
+  VK_PRESENT_MODE_IMMEDIATE_KHR = 0,
+  VK_PRESENT_MODE_MAILBOX_KHR = 1,
+  VK_PRESENT_MODE_FIFO_KHR = 2,
+  VK_PRESENT_MODE_FIFO_RELAXED_KHR = 3
+} VkPresentModeKHR;
+
+typedef enum VkSurfaceTransformFlagBitsKHR {
+  VK_SURFACE_TRANSFORM_IDENTITY_BIT_KHR = 0x00000001
+} VkSurfaceTransformFlagBitsKHR;
+typedef VkFlags VkSurfaceTransformFlagsKHR;
+
+typedef enum VkCompositeAlphaFlagBitsKHR {
+  VK_COMPOSITE_ALPHA_OPAQUE_BIT_KHR = 0x00000001
+} VkCompositeAlphaFlagBitsKHR;
+typedef VkFlags VkCompositeAlphaFlagsKHR;
+typedef VkFlags VkSwapchainCreateFlagsKHR;
+
+typedef struct VkSurfaceCapabilitiesKHR {
+  uint32_t minImageCount;
+  uint32_t maxImageCount;
+  VkExtent2D currentExtent;
+  VkExtent2D minImageExtent;
+  VkExtent2D maxImageExtent;
+  uint32_t maxImageArrayLayers;
+  VkSurfaceTransformFlagsKHR supportedTransforms;
+  VkSurfaceTransformFlagBitsKHR currentTransform;
+  VkCompositeAlphaFlagsKHR supportedCompositeAlpha;
+  VkImageUsageFlags supportedUsageFlags;
+} VkSurfaceCapabilitiesKHR;
+
+typedef struct VkSurfaceFormatKHR {
+  VkFormat format;
+  VkColorSpaceKHR colorSpace;
+} VkSurfaceFormatKHR;
+
+typedef struct VkSwapchainCreateInfoKHR {
+  VkStructureType sType;
+  const void *pNext;
+  VkSwapchainCreateFlagsKHR flags;
+  VkSurfaceKHR surface;
+  uint32_t minImageCount;
+  VkFormat imageFormat;
+  VkColorSpaceKHR imageColorSpace;
+  VkExtent2D imageExtent;
+  uint32_t imageArrayLayers;
+  VkImageUsageFlags imageUsage;
+  VkSharingMode imageSharingMode;
+  uint32_t queueFamilyIndexCount;
+  const uint32_t *pQueueFamilyIndices;
+  VkSurfaceTransformFlagBitsKHR preTransform;
+  VkCompositeAlphaFlagBitsKHR compositeAlpha;
+  VkPresentModeKHR presentMode;
+  VkBool32 clipped;
+  VkSwapchainKHR oldSwapchain;
+} VkSwapchainCreateInfoKHR;
+
+typedef struct VkPresentInfoKHR {
+  VkStructureType sType;
+  const void *pNext;
+  uint32_t waitSemaphoreCount;
+  const VkSemaphore *pWaitSemaphores;
+  uint32_t swapchainCount;
+  const VkSwapchainKHR *pSwapchains;
+  const uint32_t *pImageIndices;
+  VkResult *pResults;
+} VkPresentInfoKHR;
+
+typedef void(VKAPI_PTR *PFN_vkDestroySurfaceKHR)(VkInstance, VkSurfaceKHR, const VkAllocationCallbacks *);
+typedef VkResult(VKAPI_PTR *PFN_vkGetPhysicalDeviceSurfaceSupportKHR)(VkPhysicalDevice, uint32_t, VkSurfaceKHR, VkBool32 *);
+typedef VkResult(VKAPI_PTR *PFN_vkGetPhysicalDeviceSurfaceCapabilitiesKHR)(VkPhysicalDevice, VkSurfaceKHR, VkSurfaceCapabilitiesKHR *);
+typedef VkResult(VKAPI_PTR *PFN_vkGetPhysicalDeviceSurfaceFormatsKHR)(VkPhysicalDevice, VkSurfaceKHR, uint32_t *, VkSurfaceFormatKHR *);
+typedef VkResult(VKAPI_PTR *PFN_vkGetPhysicalDeviceSurfacePresentModesKHR)(VkPhysicalDevice, VkSurfaceKHR, uint32_t *, VkPresentModeKHR *);
+typedef VkResult(VKAPI_PTR *PFN_vkCreateSwapchainKHR)(VkDevice, const VkSwapchainCreateInfoKHR *, const VkAllocationCallbacks *, VkSwapchainKHR *);
+typedef void(VKAPI_PTR *PFN_vkDestroySwapchainKHR)(VkDevice, VkSwapchainKHR, const VkAllocationCallbacks *);
+typedef VkResult(VKAPI_PTR *PFN_vkGetSwapchainImagesKHR)(VkDevice, VkSwapchainKHR, uint32_t *, VkImage *);
+typedef VkResult(VKAPI_PTR *PFN_vkAcquireNextImageKHR)(VkDevice, VkSwapchainKHR, uint64_t, VkSemaphore, VkFence, uint32_t *);
+typedef VkResult(VKAPI_PTR *PFN_vkQueuePresentKHR)(VkQueue, const VkPresentInfoKHR *);
 typedef void(VKAPI_PTR *PFN_vkCmdPipelineBarrier)(VkCommandBuffer, VkPipelineStageFlags, VkPipelineStageFlags, VkDependencyFlags, uint32_t, const VkMemoryBarrier *, uint32_t, const VkBufferMemoryBarrier *, uint32_t, const VkImageMemoryBarrier *);
 typedef void(VKAPI_PTR *PFN_vkCmdPushConstants)(VkCommandBuffer, VkPipelineLayout, VkShaderStageFlags, uint32_t, uint32_t, const void *);
 typedef void(VKAPI_PTR *PFN_vkCmdBeginRenderPass)(VkCommandBuffer, const VkRenderPassBeginInfo *, VkSubpassContents);

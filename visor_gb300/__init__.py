@@ -24,6 +24,8 @@ MODE_PER_DRAW = 1
 
 RESTAGE_INPUTS = 1
 DEVICE_TARGETS = 2
+GPU_MIPS = 4      # upload mip 0 only and build mip chains with vkCmdBlitImage
+PRESENT = 8       # target 0 renders into a headless swapchain image and is read back from the present
 
 _lib = None
 

@@ -300,21 +300,44 @@ VISOR_EXPORT VkResult vkEnumerateInstanceVersion(uint32_t *pApiVersion)
   return VK_SUCCESS;
 }
 
-VISOR_EXPORT VkResult vkEnumerateInstanceExtensionProperties(const char *, uint32_t *pCount,
-                                                             VkExtensionProperties *)
+namespace
 {
-  /* headless: no surface extensions (WSI is replaced by mapped render targets) */
-  if(pCount)
-    *pCount = 0;
-  return VK_SUCCESS;
+VkResult list_extensions(const char *const *names, const uint32_t *specs, uint32_t n, uint32_t *pCount,
+                         VkExtensionProperties *props)
+{
+  if(!props)
+  {
+    *pCount = n;
+    return VK_SUCCESS;
+  }
+  const uint32_t k = std::min(*pCount, n);
+  for(uint32_t i = 0; i < k; i++)
+  {
+    memset(&props[i], 0, sizeof(props[i]));
+    snprintf(props[i].extensionName, sizeof(props[i].extensionName), "%s", names[i]);
+    props[i].specVersion = specs[i];
+  }
+  *pCount = k;
+  return k < n ? VK_INCOMPLETE : VK_SUCCESS;
+}
+}    // namespace
+
+/* presentation is headless: a headless surface (no window system exists on the
+   machines this runs on) and swapchains whose images stay in device memory */
+VISOR_EXPORT VkResult vkEnumerateInstanceExtensionProperties(const char *, uint32_t *pCount,
+                                                             VkExtensionProperties *props)
+{
+  static const char *const names[] = {"VK_KHR_surface", "VK_EXT_headless_surface"};
+  static const uint32_t specs[] = {25, 1};
+  return list_extensions(names, specs, 2, pCount, props);
 }
 
 VISOR_EXPORT VkResult vkEnumerateDeviceExtensionProperties(VkPhysicalDevice, const char *, uint32_t *pCount,
-                                                           VkExtensionProperties *)
+                                                           VkExtensionProperties *props)
 {
-  if(pCount)
-    *pCount = 0;
-  return VK_SUCCESS;
+  static const char *const names[] = {"VK_KHR_swapchain"};
+  static const uint32_t specs[] = {68};
+  return list_extensions(names, specs, 1, pCount, props);
 }
 
 VISOR_EXPORT VkResult vkEnumeratePhysicalDevices(VkInstance, uint32_t *pCount, VkPhysicalDevice *pDevs)
@@ -1595,6 +1618,265 @@ VISOR_EXPORT VkResult vkQueueSubmit(VkQueue q, uint32_t n, const VkSubmitInfo *s
 }
 
 /* ------------------------------------------------------------------------ */
+/* WSI, headless (wsi.cpp presents with GDI; here images stay on the device) */
+/* ------------------------------------------------------------------------ */
+
+struct VkSurfaceKHR_T
+{
+  uint32_t platform = 0; /* VkIcdSurfaceBase layout: the platform tag comes first */
+};
+
+struct VkSwapchainKHR_T
+{
+  struct Backbuffer
+  {
+    VkImage_T *im = nullptr;
+    VkDeviceMemory_T *mem = nullptr;
+    void *presented = nullptr; /* pinned host copy of the last present */
+    vgpu_list *present = nullptr;
+  };
+  std::vector<Backbuffer> backbuffers;
+  VkExtent2D extent = {0, 0};
+  VkQueue_T *queue = nullptr;
+  uint32_t current = 0;
+  uint64_t frames = 0;
+};
+
+namespace
+{
+constexpr uint32_t kHeadlessPlatform = 10; /* VK_ICD_WSI_PLATFORM_HEADLESS */
+}
+
+VISOR_EXPORT VkResult vkCreateHeadlessSurfaceEXT(VkInstance, const VisorHeadlessSurfaceCreateInfoEXT *,
+                                                 const VkAllocationCallbacks *, VkSurfaceKHR *pSurface)
+{
+  VkSurfaceKHR_T *sf = new VkSurfaceKHR_T();
+  sf->platform = kHeadlessPlatform;
+  *pSurface = sf;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroySurfaceKHR(VkInstance, VkSurfaceKHR surface, const VkAllocationCallbacks *)
+{
+  delete surface;
+}
+
+/* wsi.cpp:3-12: every queue presents */
+VISOR_EXPORT VkResult vkGetPhysicalDeviceSurfaceSupportKHR(VkPhysicalDevice, uint32_t, VkSurfaceKHR,
+                                                           VkBool32 *pSupported)
+{
+  if(pSupported)
+    *pSupported = VK_TRUE;
+  return VK_SUCCESS;
+}
+
+/* wsi.cpp:14-32: BGRA8 in SRGB and UNORM */
+VISOR_EXPORT VkResult vkGetPhysicalDeviceSurfaceFormatsKHR(VkPhysicalDevice, VkSurfaceKHR, uint32_t *pCount,
+                                                           VkSurfaceFormatKHR *pFormats)
+{
+  const VkFormat fmts[2] = {VK_FORMAT_B8G8R8A8_SRGB, VK_FORMAT_B8G8R8A8_UNORM};
+  if(!pFormats)
+  {
+    *pCount = 2;
+    return VK_SUCCESS;
+  }
+  const uint32_t n = std::min<uint32_t>(*pCount, 2);
+  for(uint32_t i = 0; i < n; i++)
+  {
+    pFormats[i].format = fmts[i];
+    pFormats[i].colorSpace = VK_COLOR_SPACE_SRGB_NONLINEAR_KHR;
+  }
+  *pCount = n;
+  return n < 2 ? VK_INCOMPLETE : VK_SUCCESS;
+}
+
+/* wsi.cpp:34-68 with no window: the swapchain decides the extent */
+VISOR_EXPORT VkResult vkGetPhysicalDeviceSurfaceCapabilitiesKHR(VkPhysicalDevice, VkSurfaceKHR,
+                                                                VkSurfaceCapabilitiesKHR *c)
+{
+  memset(c, 0, sizeof(*c));
+  c->minImageCount = 1;
+  c->maxImageCount = 3;
+  c->currentExtent = {0xFFFFFFFFu, 0xFFFFFFFFu};
+  c->minImageExtent = {1, 1};
+  c->maxImageExtent = {16384, 16384};
+  c->maxImageArrayLayers = 1;
+  c->supportedTransforms = VK_SURFACE_TRANSFORM_IDENTITY_BIT_KHR;
+  c->currentTransform = VK_SURFACE_TRANSFORM_IDENTITY_BIT_KHR;
+  c->supportedCompositeAlpha = VK_COMPOSITE_ALPHA_OPAQUE_BIT_KHR;
+  c->supportedUsageFlags = VK_IMAGE_USAGE_TRANSFER_SRC_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT |
+                           VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT;
+  return VK_SUCCESS;
+}
+
+/* wsi.cpp:70-84: FIFO only */
+VISOR_EXPORT VkResult vkGetPhysicalDeviceSurfacePresentModesKHR(VkPhysicalDevice, VkSurfaceKHR, uint32_t *pCount,
+                                                                VkPresentModeKHR *pModes)
+{
+  if(!pModes)
+  {
+    *pCount = 1;
+    return VK_SUCCESS;
+  }
+  if(*pCount >= 1)
+  {
+    pModes[0] = VK_PRESENT_MODE_FIFO_KHR;
+    *pCount = 1;
+  }
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroySwapchainKHR(VkDevice, VkSwapchainKHR sc, const VkAllocationCallbacks *);
+
+/* wsi.cpp:86-149: minImageCount backbuffers of the requested extent; here in device
+   memory, each with a pinned host copy that a present fills */
+VISOR_EXPORT VkResult vkCreateSwapchainKHR(VkDevice dev, const VkSwapchainCreateInfoKHR *info,
+                                           const VkAllocationCallbacks *, VkSwapchainKHR *pSwapchain)
+{
+  VkSwapchainKHR_T *sc = new VkSwapchainKHR_T();
+  sc->extent = info->imageExtent;
+  sc->queue = dev->queue;
+  sc->backbuffers.resize(std::max(1u, info->minImageCount));
+  const uint64_t bytes = (uint64_t)sc->extent.width * sc->extent.height * 4;
+  for(auto &b : sc->backbuffers)
+  {
+    b.mem = new VkDeviceMemory_T();
+    b.mem->size = bytes;
+    b.mem->type = 0;
+    int rc = vgpu_mem_alloc(bytes, 0, &b.mem->dptr, nullptr);
+    if(!rc)
+      rc = vgpu_host_alloc(bytes, &b.presented);
+    if(rc)
+    {
+      vkDestroySwapchainKHR(dev, sc, nullptr);
+      return vr(rc);
+    }
+    b.im = new VkImage_T();
+    b.im->extent = {sc->extent.width, sc->extent.height, 1};
+    b.im->format = info->imageFormat;
+    b.im->bpp = 4;
+    b.im->mem = b.mem;
+    b.present = vgpu_list_create();
+    vgpu_list_download(b.present, b.presented, b.mem->dptr, bytes);
+  }
+  *pSwapchain = sc;
+  return VK_SUCCESS;
+}
+
+VISOR_EXPORT void vkDestroySwapchainKHR(VkDevice, VkSwapchainKHR sc, const VkAllocationCallbacks *)
+{
+  if(!sc)
+    return;
+  if(sc->queue)
+    vgpu_queue_wait_idle(sc->queue->q);
+  for(auto &b : sc->backbuffers)
+  {
+    vgpu_list_destroy(b.present);
+    if(b.mem)
+      vgpu_mem_free(b.mem->dptr, nullptr);
+    vgpu_host_free(b.presented);
+    delete b.mem;
+    delete b.im;
+  }
+  delete sc;
+}
+
+/* wsi.cpp:174-188 */
+VISOR_EXPORT VkResult vkGetSwapchainImagesKHR(VkDevice, VkSwapchainKHR sc, uint32_t *pCount, VkImage *pImages)
+{
+  if(!pImages)
+  {
+    *pCount = (uint32_t)sc->backbuffers.size();
+    return VK_SUCCESS;
+  }
+  const uint32_t n = std::min<uint32_t>(*pCount, (uint32_t)sc->backbuffers.size());
+  for(uint32_t i = 0; i < n; i++)
+    pImages[i] = sc->backbuffers[i].im;
+  *pCount = n;
+  return n < sc->backbuffers.size() ? VK_INCOMPLETE : VK_SUCCESS;
+}
+
+/* wsi.cpp:190-199: round robin; the image is free at once, so a fence is signalled */
+VISOR_EXPORT VkResult vkAcquireNextImageKHR(VkDevice, VkSwapchainKHR sc, uint64_t, VkSemaphore, VkFence fence,
+                                            uint32_t *pIndex)
+{
+  sc->current = (sc->current + 1) % (uint32_t)sc->backbuffers.size();
+  *pIndex = sc->current;
+  if(fence)
+    vgpu_fence_reset(fence->f);
+  return VK_SUCCESS;
+}
+
+/* wsi.cpp:201-220 BitBlts to the window; here the image is copied to its pinned
+   host copy in queue order, and written as a PPM file when VISOR_GB300_PRESENT_DIR
+   names a directory */
+VISOR_EXPORT VkResult vkQueuePresentKHR(VkQueue q, const VkPresentInfoKHR *info)
+{
+  const char *dir = getenv("VISOR_GB300_PRESENT_DIR");
+  VkResult res = VK_SUCCESS;
+  for(uint32_t i = 0; i < info->swapchainCount; i++)
+  {
+    VkSwapchainKHR_T *sc = info->pSwapchains[i];
+    const uint32_t idx = info->pImageIndices[i];
+    VkResult r = VK_SUCCESS;
+    if(idx >= sc->backbuffers.size())
+      r = VK_ERROR_OUT_OF_DATE_KHR;
+    else
+    {
+      int rc = vgpu_submit(q->q, sc->backbuffers[idx].present);
+      if(!rc && dir && *dir)
+      {
+        rc = vgpu_queue_wait_idle(q->q);
+        char path[4096];
+        snprintf(path, sizeof(path), "%s/frame_%06llu.ppm", dir, (unsigned long long)sc->frames);
+        if(FILE *fh = fopen(path, "wb"))
+        {
+          const uint32_t w = sc->extent.width, h = sc->extent.height;
+          fprintf(fh, "P6\n%u %u\n255\n", w, h);
+          const uint8_t *px = (const uint8_t *)sc->backbuffers[idx].presented;
+          std::vector<uint8_t> row((size_t)w * 3);
+          for(uint32_t y = 0; y < h; y++)
+          {
+            for(uint32_t x = 0; x < w; x++)
+            {
+              const uint8_t *p = px + ((size_t)y * w + x) * 4; /* B, G, R, A */
+              row[x * 3 + 0] = p[2];
+              row[x * 3 + 1] = p[1];
+              row[x * 3 + 2] = p[0];
+            }
+            fwrite(row.data(), 1, row.size(), fh);
+          }
+          fclose(fh);
+        }
+      }
+      r = vr(rc);
+      sc->frames++;
+    }
+    if(info->pResults)
+      info->pResults[i] = r;
+    if(r != VK_SUCCESS)
+      res = r;
+  }
+  return res;
+}
+
+/* Copy the last presented contents of swapchain image `index` (BGRA8, width*height*4
+   bytes) to dst, after the queue has finished presenting it. */
+VISOR_EXPORT VkResult visor_gb300_swapchain_read(VkSwapchainKHR sc, uint32_t index, void *dst, size_t size)
+{
+  if(!sc || index >= sc->backbuffers.size())
+    return VK_ERROR_INITIALIZATION_FAILED;
+  const size_t bytes = (size_t)sc->extent.width * sc->extent.height * 4;
+  if(size < bytes)
+    return VK_INCOMPLETE;
+  int rc = vgpu_queue_wait_idle(sc->queue->q);
+  if(rc)
+    return vr(rc);
+  memcpy(dst, sc->backbuffers[index].presented, bytes);
+  return VK_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------ */
 /* loader interface (icd_interface.cpp)                                     */
 /* ------------------------------------------------------------------------ */
 
@@ -1611,6 +1893,7 @@ struct Entry
 };
 
 const Entry kInstanceFns[] = {
+    ICD_ENTRY(vkCreateHeadlessSurfaceEXT), ICD_ENTRY(vkDestroySurfaceKHR),
     ICD_ENTRY(vkEnumerateInstanceExtensionProperties), ICD_ENTRY(vkEnumerateDeviceExtensionProperties),
     ICD_ENTRY(vkGetDeviceProcAddr), ICD_ENTRY(vkCreateInstance), ICD_ENTRY(vkDestroyInstance),
     ICD_ENTRY(vkEnumeratePhysicalDevices), ICD_ENTRY(vkCreateDevice), ICD_ENTRY(vkEnumerateInstanceVersion),
@@ -1619,10 +1902,14 @@ const Entry kInstanceFns[] = {
 const Entry kPhysFns[] = {
     ICD_ENTRY(vkGetPhysicalDeviceFeatures), ICD_ENTRY(vkGetPhysicalDeviceProperties),
     ICD_ENTRY(vkGetPhysicalDeviceQueueFamilyProperties), ICD_ENTRY(vkGetPhysicalDeviceMemoryProperties),
-    ICD_ENTRY(vkGetPhysicalDeviceFormatProperties),
+    ICD_ENTRY(vkGetPhysicalDeviceFormatProperties), ICD_ENTRY(vkGetPhysicalDeviceSurfaceSupportKHR),
+    ICD_ENTRY(vkGetPhysicalDeviceSurfaceCapabilitiesKHR), ICD_ENTRY(vkGetPhysicalDeviceSurfaceFormatsKHR),
+    ICD_ENTRY(vkGetPhysicalDeviceSurfacePresentModesKHR),
 };
 
 const Entry kDeviceFns[] = {
+    ICD_ENTRY(vkCreateSwapchainKHR), ICD_ENTRY(vkDestroySwapchainKHR), ICD_ENTRY(vkGetSwapchainImagesKHR),
+    ICD_ENTRY(vkAcquireNextImageKHR), ICD_ENTRY(vkQueuePresentKHR),
     ICD_ENTRY(vkDestroyDevice), ICD_ENTRY(vkGetDeviceQueue), ICD_ENTRY(vkCreateFence), ICD_ENTRY(vkDestroyFence),
     ICD_ENTRY(vkCreateSemaphore), ICD_ENTRY(vkDestroySemaphore), ICD_ENTRY(vkCreateCommandPool),
     ICD_ENTRY(vkDestroyCommandPool), ICD_ENTRY(vkAllocateCommandBuffers), ICD_ENTRY(vkFreeCommandBuffers),

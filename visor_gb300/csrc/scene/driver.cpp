@@ -113,6 +113,10 @@ struct vsd_scene
   VkCommandBuffer cmd = VK_NULL_HANDLE;
   VkFence fence = VK_NULL_HANDLE;
   uint64_t restage_bytes = 0;
+  /* VSD_PRESENT: headless surface and swapchain owning target 0's colour image */
+  VkSurfaceKHR surface = VK_NULL_HANDLE;
+  VkSwapchainKHR swapchain = VK_NULL_HANDLE;
+  uint32_t image_index = 0;
 };
 
 #define VSD_CHECK(expr)          \
@@ -481,6 +485,59 @@ static int record(vsd_scene *s)
   return 0;
 }
 
+/* VSD_PRESENT: a headless surface, a two-image BGRA8 swapchain of target 0's size,
+   and a view of the acquired image as the colour attachment */
+static int make_swapchain_target(vsd_scene *s, TargetObjs &o)
+{
+#ifdef VISOR_DRIVER_KHRONOS_HEADER
+  (void)s, (void)o;
+  return VK_ERROR_EXTENSION_NOT_PRESENT; /* the reference presents only to Win32 windows */
+#else
+  vsd_context *c = s->ctx;
+  auto create_surface =
+      (PFN_vkCreateHeadlessSurfaceEXT_visor)c->gpa(c->instance, "vkCreateHeadlessSurfaceEXT");
+  auto create_swapchain = (PFN_vkCreateSwapchainKHR)c->gpa(c->instance, "vkCreateSwapchainKHR");
+  auto get_images = (PFN_vkGetSwapchainImagesKHR)c->gpa(c->instance, "vkGetSwapchainImagesKHR");
+  auto acquire = (PFN_vkAcquireNextImageKHR)c->gpa(c->instance, "vkAcquireNextImageKHR");
+  if(!create_surface || !create_swapchain || !get_images || !acquire)
+    return VK_ERROR_EXTENSION_NOT_PRESENT;
+  VisorHeadlessSurfaceCreateInfoEXT hci = {};
+  hci.sType = (VkStructureType)VISOR_STRUCTURE_TYPE_HEADLESS_SURFACE_CREATE_INFO_EXT;
+  VSD_CHECK(create_surface(c->instance, &hci, nullptr, &s->surface));
+  VkSwapchainCreateInfoKHR sci = {};
+  sci.sType = VK_STRUCTURE_TYPE_SWAPCHAIN_CREATE_INFO_KHR;
+  sci.surface = s->surface;
+  sci.minImageCount = 2;
+  sci.imageFormat = VK_FORMAT_B8G8R8A8_UNORM;
+  sci.imageColorSpace = VK_COLOR_SPACE_SRGB_NONLINEAR_KHR;
+  sci.imageExtent.width = o.width;
+  sci.imageExtent.height = o.height;
+  sci.imageArrayLayers = 1;
+  sci.imageUsage = VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT;
+  sci.preTransform = VK_SURFACE_TRANSFORM_IDENTITY_BIT_KHR;
+  sci.compositeAlpha = VK_COMPOSITE_ALPHA_OPAQUE_BIT_KHR;
+  sci.presentMode = VK_PRESENT_MODE_FIFO_KHR;
+  sci.clipped = VK_TRUE;
+  VSD_CHECK(create_swapchain(c->device, &sci, nullptr, &s->swapchain));
+  uint32_t n = 0;
+  VSD_CHECK(get_images(c->device, s->swapchain, &n, nullptr));
+  std::vector<VkImage> images(n);
+  VSD_CHECK(get_images(c->device, s->swapchain, &n, images.data()));
+  VSD_CHECK(acquire(c->device, s->swapchain, ~0ull, VK_NULL_HANDLE, VK_NULL_HANDLE, &s->image_index));
+  VkImageViewCreateInfo vci = {};
+  vci.sType = VK_STRUCTURE_TYPE_IMAGE_VIEW_CREATE_INFO;
+  vci.image = images[s->image_index];
+  vci.viewType = VK_IMAGE_VIEW_TYPE_2D;
+  vci.format = VK_FORMAT_B8G8R8A8_UNORM;
+  vci.subresourceRange.aspectMask = VK_IMAGE_ASPECT_COLOR_BIT;
+  vci.subresourceRange.levelCount = 1;
+  vci.subresourceRange.layerCount = 1;
+  VSD_CHECK(c->fn.vkCreateImageView(c->device, &vci, nullptr, &o.color_view));
+  o.color = VK_NULL_HANDLE; /* owned by the swapchain */
+  return 0;
+#endif
+}
+
 static int submit_one(vsd_scene *s, VkCommandBuffer cmd)
 {
   Fns &f = s->ctx->fn;
@@ -489,6 +546,16 @@ static int submit_one(vsd_scene *s, VkCommandBuffer cmd)
   si.commandBufferCount = 1;
   si.pCommandBuffers = &cmd;
   VSD_CHECK(f.vkQueueSubmit(s->ctx->queue, 1, &si, s->fence));
+  if(s->swapchain && cmd == s->cmd)
+  {
+    auto present = (PFN_vkQueuePresentKHR)s->ctx->gpa(s->ctx->instance, "vkQueuePresentKHR");
+    VkPresentInfoKHR pi = {};
+    pi.sType = VK_STRUCTURE_TYPE_PRESENT_INFO_KHR;
+    pi.swapchainCount = 1;
+    pi.pSwapchains = &s->swapchain;
+    pi.pImageIndices = &s->image_index;
+    VSD_CHECK(present(s->ctx->queue, &pi));
+  }
   VSD_CHECK(f.vkWaitForFences(s->ctx->device, 1, &s->fence, VK_TRUE, ~0ull));
   VSD_CHECK(f.vkResetFences(s->ctx->device, 1, &s->fence));
   return 0;
@@ -569,9 +636,12 @@ extern "C" int vsd_upload(vsd_context *c, const vsc_scene *sc, uint32_t flags, v
     TargetObjs &o = s->targets[t];
     o.width = sc->targets[t].width;
     o.height = sc->targets[t].height;
-    TRY(make_image(c, o.width, o.height, 1, VK_FORMAT_R8G8B8A8_UNORM,
-                   VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT, ttype, VK_IMAGE_ASPECT_COLOR_BIT, &o.color,
-                   &o.color_mem, &o.color_view));
+    if(t == 0 && (flags & VSD_PRESENT))
+      TRY(make_swapchain_target(s, o));
+    else
+      TRY(make_image(c, o.width, o.height, 1, VK_FORMAT_R8G8B8A8_UNORM,
+                     VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT, ttype, VK_IMAGE_ASPECT_COLOR_BIT, &o.color,
+                     &o.color_mem, &o.color_view));
     TRY(make_image(c, o.width, o.height, 1, VK_FORMAT_D32_SFLOAT,
                    VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT, ttype, VK_IMAGE_ASPECT_DEPTH_BIT,
                    &o.depth, &o.depth_mem, &o.depth_view));
@@ -745,7 +815,13 @@ extern "C" int vsd_read_target(vsd_scene *s, uint32_t target, uint8_t *color, fl
   TargetObjs &t = s->targets[target];
   VkDeviceSize bytes = (VkDeviceSize)t.width * t.height * 4;
   void *p = nullptr;
-  if(color)
+  if(color && target == 0 && s->swapchain)
+  {
+#ifndef VISOR_DRIVER_KHRONOS_HEADER
+    VSD_CHECK(visor_gb300_swapchain_read(s->swapchain, s->image_index, color, (size_t)bytes));
+#endif
+  }
+  else if(color)
   {
     VSD_CHECK(c->fn.vkMapMemory(c->device, t.color_mem.mem, 0, bytes, 0, &p));
     memcpy(color, p, (size_t)bytes);
@@ -782,6 +858,16 @@ extern "C" void vsd_release(vsd_scene *s)
     if(t.depth) f.vkDestroyImage(d, t.depth, nullptr);
     if(t.color_mem.mem) f.vkFreeMemory(d, t.color_mem.mem, nullptr);
     if(t.depth_mem.mem) f.vkFreeMemory(d, t.depth_mem.mem, nullptr);
+  }
+  if(s->swapchain)
+  {
+    auto destroy = (PFN_vkDestroySwapchainKHR)c->gpa(c->instance, "vkDestroySwapchainKHR");
+    destroy(d, s->swapchain, nullptr);
+  }
+  if(s->surface)
+  {
+    auto destroy = (PFN_vkDestroySurfaceKHR)c->gpa(c->instance, "vkDestroySurfaceKHR");
+    destroy(c->instance, s->surface, nullptr);
   }
   for(TextureObjs &t : s->textures)
   {
