@@ -413,14 +413,23 @@ __device__ __forceinline__ float vgx_plane_depth(const VgxPlane &p, int dx, int 
          n[2] * __uint_as_float(p.d.z);
 }
 
+#define VGX_QCAP 64
+
 /* Per-warp shared memory.  Planes are stored as separate arrays of uint4 so
    that lanes reading different triangles' planes hit different banks. */
 struct VgxWarpShared
 {
   uint4 pe[32], pa[32], pb[32], pd[32];
   float4 col[32];
-  u32 frag[32]; /* fragment window: triangle | pixel-half << 5 | owner lane << 6 (deferred: record) */
+  u32 frag[32]; /* deferred window: triangle record */
   u32 fown[32]; /* deferred window: owner lane | pixel-half << 5 */
+#if !VGX_DEFERRED
+  /* fragment queue: passing fragments wait here across batches until 32 can be
+     shaded at once; in queue order, so each pixel's fragments stay in primitive order */
+  u32 qrec[VGX_QCAP], qown[VGX_QCAP], qst[VGX_QCAP];
+  int qb[3][VGX_QCAP]; /* barycentric edge values at the fragment's pixel */
+  u32 omask[32];       /* per owner lane: its entries of the window being blended */
+#endif
 };
 
 __device__ __forceinline__ VgxPlane vgx_plane_load(const VgxWarpShared &sh, u32 t)
@@ -433,6 +442,91 @@ __device__ __forceinline__ VgxPlane vgx_plane_load(const VgxWarpShared &sh, u32 
   return p;
 }
 
+#if !VGX_DEFERRED
+/*
+ * Shade the first cnt (<= 32) queued fragments, one per lane, then let each
+ * pixel's owner lane blend its entries in queue order, and drop them from the
+ * queue (qn -= cnt, later entries move to the front).
+ */
+__device__ __forceinline__ void vgx_queue_shade(const VgxJob &job, VgxWarpShared &sh, int lane,
+                                                u32 cnt, u32 *col, u32 &qn)
+{
+  const VgxDraw *draws = (const VgxDraw *)job.draws;
+  const bool live = (u32)lane < cnt;
+  if(live)
+  {
+    const u32 *g = (const u32 *)job.records + (u64)sh.qrec[lane] * VGX_REC;
+    const float ia = __uint_as_float(__ldg(g + R_INVAREA));
+    float nb[4];
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+      nb[k] = (float)sh.qb[k][lane] * ia;
+    /* perspective correction, rasterizer.cpp:580-588 */
+    nb[0] = nb[0] * __uint_as_float(__ldg(g + R_INVW));
+    nb[1] = nb[1] * __uint_as_float(__ldg(g + R_INVW + 1));
+    nb[2] = nb[2] * __uint_as_float(__ldg(g + R_INVW + 2));
+    const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
+    nb[0] = nb[0] * invlen;
+    nb[1] = nb[1] * invlen;
+    nb[2] = nb[2] * invlen;
+    nb[3] = 0.0f;
+    float iv[3 * (VGX_K > 0 ? VGX_K : 1)];
+#pragma unroll
+    for(int q = 0; q < 3 * VGX_K; q++)
+      iv[q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + q));
+    sh.col[lane] = vgx_fs(draws[__ldg(g + R_DRAW)], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
+                          __uint_as_float(__ldg(g + R_LOD)));
+  }
+  /* each owner learns which window entries are its own */
+  const u32 own = live ? (sh.qown[lane] & 31u) : 32u + (u32)lane;
+  sh.omask[lane] = 0;
+  __syncwarp();
+  const u32 peers = __match_any_sync(0xffffffffu, own);
+  if(live)
+    sh.omask[own] = peers;
+  __syncwarp();
+  u32 m = sh.omask[lane];
+  while(m)
+  {
+    const u32 i = (u32)(__ffs(m) - 1);
+    m &= m - 1;
+    const float4 c = sh.col[i];
+    const u32 st = sh.qst[i];
+    if(sh.qown[i] & 32u)
+      col[1] = vgx_blend_write(st, c, col[1]);
+    else
+      col[0] = vgx_blend_write(st, c, col[0]);
+  }
+  __syncwarp();
+  /* move the rest of the queue to the front */
+  const u32 rest = qn - cnt;
+  u32 r_rec = 0, r_own = 0, r_st = 0;
+  int r_b[3] = {0, 0, 0};
+  const bool mv = (u32)lane < rest;
+  if(mv)
+  {
+    r_rec = sh.qrec[cnt + lane];
+    r_own = sh.qown[cnt + lane];
+    r_st = sh.qst[cnt + lane];
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+      r_b[k] = sh.qb[k][cnt + lane];
+  }
+  __syncwarp();
+  if(mv)
+  {
+    sh.qrec[lane] = r_rec;
+    sh.qown[lane] = r_own;
+    sh.qst[lane] = r_st;
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+      sh.qb[k][lane] = r_b[k];
+  }
+  __syncwarp();
+  qn = rest;
+}
+#endif
+
 /*
  * One warp, one 8x8 sub-tile at (x0, y0), one batch of n <= 32 triangles whose
  * record headers lane t holds in r[] (triangle t).  Lane L owns pixels
@@ -442,8 +536,8 @@ __device__ __forceinline__ VgxPlane vgx_plane_load(const VgxWarpShared &sh, u32 
 __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShared &sh, int lane,
                                                   u32 n, const int *r, u32 rec_index, int x0, int y0,
                                                   const bool *in, u32 *col, float *dep, u32 *vis,
-                                                  u64 &covered_total, u64 &shaded_total,
-                                                  u64 &tested_total)
+                                                  u32 &qn, bool last, u64 &covered_total,
+                                                  u64 &shaded_total, u64 &tested_total)
 {
   const VgxDraw *draws = (const VgxDraw *)job.draws;
   const int ldx = lane & 7, ldy = lane >> 3;
@@ -648,81 +742,47 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
   }
   const u32 total = __shfl_sync(0xffffffffu, incl, 31);
   const u32 excl = incl - mine;
-  u32 wm0 = pass[0], wm1 = pass[1]; /* fragments not yet placed in a window */
-  u32 bm0 = pass[0], bm1 = pass[1]; /* fragments not yet blended */
-  u32 wnext = excl, bnext = excl;
-
-  for(u32 chunk = 0; chunk < total; chunk += 32)
+  /* append this batch's fragments to the queue (lane by lane, each lane's first
+     pixel then its second, triangles ascending); shade every full window */
+  u32 m0 = pass[0], m1 = pass[1];
+  u32 f = excl; /* batch index of this lane's next fragment */
+  for(u32 done = 0, once = 1; done < total || once; once = 0)
   {
-    /* place this lane's fragments that fall into the window [chunk, chunk + 32) */
-    while(wnext < excl + mine && wnext < chunk + 32)
-    {
-      u32 e;
-      if(wm0)
-      {
-        e = (u32)(__ffs(wm0) - 1);
-        wm0 &= wm0 - 1;
-      }
-      else
-      {
-        e = (u32)(__ffs(wm1) - 1) | 32u;
-        wm1 &= wm1 - 1;
-      }
-      sh.frag[wnext - chunk] = e | ((u32)lane << 6);
-      wnext++;
-    }
-    __syncwarp();
-    if(chunk + lane < total)
-    {
-      const u32 e = sh.frag[lane];
-      const u32 t = e & 31u, sel = (e >> 5) & 1u, owner = e >> 6;
-      const int fdx = (int)(owner & 7), fdy = (int)(owner >> 3) + 4 * (int)sel;
-      const VgxPlane pt = vgx_plane_load(sh, t);
-      const u32 *g = (const u32 *)job.records + (u64)pt.b.w * VGX_REC;
-      float nb[4];
-      (void)vgx_plane_depth(pt, fdx, fdy, nb);
-      /* perspective correction, rasterizer.cpp:580-588 */
-      nb[0] = nb[0] * __uint_as_float(__ldg(g + R_INVW));
-      nb[1] = nb[1] * __uint_as_float(__ldg(g + R_INVW + 1));
-      nb[2] = nb[2] * __uint_as_float(__ldg(g + R_INVW + 2));
-      const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
-      nb[0] = nb[0] * invlen;
-      nb[1] = nb[1] * invlen;
-      nb[2] = nb[2] * invlen;
-      nb[3] = 0.0f;
-      float iv[3 * (VGX_K > 0 ? VGX_K : 1)];
-#pragma unroll
-      for(int q = 0; q < 3 * VGX_K; q++)
-        iv[q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + q));
-      sh.col[lane] = vgx_fs(draws[__ldg(g + R_DRAW)], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
-                            __uint_as_float(__ldg(g + R_LOD)));
-    }
-    __syncwarp();
-    /* in-order blend: each owner consumes its fragments of this window */
-    while(bnext < excl + mine && bnext < chunk + 32)
+    const u32 take = min((u32)VGX_QCAP - qn, total - done);
+    while(f < excl + mine && f < done + take)
     {
       u32 t, sel;
-      if(bm0)
+      if(m0)
       {
-        t = (u32)(__ffs(bm0) - 1);
-        bm0 &= bm0 - 1;
+        t = (u32)(__ffs(m0) - 1);
+        m0 &= m0 - 1;
         sel = 0;
       }
       else
       {
-        t = (u32)(__ffs(bm1) - 1);
-        bm1 &= bm1 - 1;
+        t = (u32)(__ffs(m1) - 1);
+        m1 &= m1 - 1;
         sel = 1;
       }
-      const float4 c = sh.col[bnext - chunk];
-      const u32 stt = sh.pe[t].w;
-      if(sel == 0)
-        col[0] = vgx_blend_write(stt, c, col[0]);
-      else
-        col[1] = vgx_blend_write(stt, c, col[1]);
-      bnext++;
+      const u32 slot = qn + (f - done);
+      const VgxPlane pt = vgx_plane_load(sh, t);
+      const int dy = ldy + 4 * (int)sel;
+      sh.qrec[slot] = pt.b.w;
+      sh.qown[slot] = (u32)lane | (sel << 5);
+      sh.qst[slot] = pt.e.w;
+#pragma unroll
+      for(int k = 0; k < 3; k++)
+        sh.qb[k][slot] = vgx_edge(pt, k, ldx, dy);
+      f++;
     }
+    qn += take;
+    done += take;
     __syncwarp();
+    /* full windows; the queue is drained (partial windows too) once the batch is placed
+       when it is the bin's last, or always with several sub-tiles a warp */
+    const bool drain = done >= total && (last || VGX_SUBS_PER_WARP > 1);
+    while(qn >= 32 || (drain && qn))
+      vgx_queue_shade(job, sh, lane, min(qn, 32u), col, qn);
   }
 #endif
 }
@@ -880,6 +940,7 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
     u32 col[VGX_SUBS_PER_WARP][2];
     float dep[VGX_SUBS_PER_WARP][2];
     u32 vis[VGX_SUBS_PER_WARP][2]; /* deferred fragment (record) per pixel, all-opaque jobs */
+    u32 qn = 0;                     /* fragments waiting in the warp's queue */
 #pragma unroll
     for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
     {
@@ -935,7 +996,8 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
       for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
         if(valid[j])
           vgx_subtile_batch(job, sh, lane, n, r, rec_index, sx[j], sy[j], in[j], col[j], dep[j],
-                            vis[j], covered_total, shaded_total, tested_total);
+                            vis[j], qn, base + 32 >= end, covered_total, shaded_total,
+                            tested_total);
     }
 #if VGX_DEFERRED
 #pragma unroll
