@@ -144,6 +144,9 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
   const bool live = tri < job.num_tris;
   u32 *counts = (u32 *)job.counts;
   u32 keep = 0, tested = 0;
+  int r[VGX_REC_HEAD] = {0}; /* the triangle's record header when has_rec */
+  bool has_rec = false;
+  u32 ntiles = 0;
   if(live)
   {
     u32 di = s_draw;
@@ -171,7 +174,6 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
       wy[k] = (int)((pos[k].y * -1.0f / pos[k].w + 1.0f) * 0.5f * (float)T.height);
     }
     int area2 = (wx[1] - wx[0]) * (wy[2] - wy[0]) - (wy[1] - wy[0]) * (wx[2] - wx[0]);
-    u32 ntiles = 0;
     if(area2 != 0 && !bad)
     {
       int area2_flipped = area2, barymul = 1;
@@ -202,7 +204,7 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
         if(maxx > minx && maxy > miny)
         {
           tested = (u32)(maxx - minx) * (u32)(maxy - miny);
-          int r[VGX_REC_HEAD];
+          has_rec = true;
           r[R_V0X] = wx[0];
           r[R_V0Y] = wy[0];
           r[R_ABX] = wx[1] - wx[0];
@@ -252,12 +254,21 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
             for(int j = 0; j < VGX_K; j++)
               rec[VGX_REC_HEAD + k * VGX_K + j] = __float_as_uint(iv[k][j]);
 #endif
-          ntiles = vgx_count_tiles(r);
         }
       }
     }
-    counts[tri] = ntiles;
   }
+  /* tiles touched: a thread walks a small triangle's tiles, the warp a big one's */
+  const bool big = has_rec && vgx_bbox_tiles(r, VGX_TILE_SHIFT) > VGX_COOP_TILES;
+  if(has_rec && !big)
+    ntiles = vgx_count_tiles(r);
+  const u32 none[4] = {0u, 0u, 0u, 0u};
+  const u32 coop = vgx_coop_visit_tiles(r, big, VGX_TILE_SHIFT, (int)(threadIdx.x & 31), none,
+                                        [](const u32 *, u32, int, int) {});
+  if(big)
+    ntiles = coop;
+  if(live)
+    counts[tri] = ntiles;
   u64 *cnt = (u64 *)job.counters;
   u32 kb = __ballot_sync(0xffffffffu, keep);
   if((threadIdx.x & 31) == 0 && kb)

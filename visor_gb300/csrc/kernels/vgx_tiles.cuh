@@ -81,4 +81,72 @@ __device__ __forceinline__ u32 vgx_visit_tiles(const int *r, u32 shift, F fn)
   return c;
 }
 
+/* bin tiles the record's pixel rectangle spans (tested or not) */
+__device__ __forceinline__ u32 vgx_bbox_tiles(const int *r, u32 shift)
+{
+  const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
+  const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
+  return (u32)(((maxx - 1) >> shift) - (minx >> shift) + 1) * (u32)(((maxy - 1) >> shift) - (miny >> shift) + 1);
+}
+
+/* triangles spanning more bin tiles than this are walked by the whole warp */
+#define VGX_COOP_TILES 8u
+
+/*
+ * Warp-cooperative form of vgx_visit_tiles for the lanes with `big` set (all 32
+ * lanes must call it): each such lane's triangle is walked by every lane, 32
+ * tiles at a time in row-major order, and fn(pay, index, tx, ty) runs on the
+ * lane that tested the tile, with the same index vgx_visit_tiles would give and
+ * pay[0..3] the owning lane's payload words.  Returns the calling lane's own
+ * tile count (0 when it is not big).
+ */
+template <typename F>
+__device__ __forceinline__ u32 vgx_coop_visit_tiles(const int *r, bool big, u32 shift, int lane,
+                                                    const u32 *payload, F fn)
+{
+  u32 mine = 0;
+  u32 pending = __ballot_sync(0xffffffffu, big);
+  const u32 lt = (1u << lane) - 1u;
+  while(pending)
+  {
+    const int src = __ffs(pending) - 1;
+    pending &= pending - 1;
+    int h[10];
+#pragma unroll
+    for(int i = 0; i < 10; i++)
+      h[i] = __shfl_sync(0xffffffffu, r[i], src);
+    u32 pay[4];
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+      pay[i] = __shfl_sync(0xffffffffu, payload[i], src);
+    const int minx = h[R_MIN] & 0xffff, miny = (int)((u32)h[R_MIN] >> 16);
+    const int maxx = h[R_MAX] & 0xffff, maxy = (int)((u32)h[R_MAX] >> 16);
+    const int tx0 = minx >> shift, tx1 = (maxx - 1) >> shift;
+    const int ty0 = miny >> shift, ty1 = (maxy - 1) >> shift;
+    const u32 bw = (u32)(tx1 - tx0 + 1), nt = bw * (u32)(ty1 - ty0 + 1);
+    u32 base = 0;
+    for(u32 k = 0; k < nt; k += 32)
+    {
+      const u32 i = k + (u32)lane;
+      bool hit = false;
+      int tx = 0, ty = 0;
+      if(i < nt)
+      {
+        tx = tx0 + (int)(i % bw);
+        ty = ty0 + (int)(i / bw);
+        const int x0 = max(minx, tx << shift), x1 = min(maxx, (tx + 1) << shift) - 1;
+        const int y0 = max(miny, ty << shift), y1 = min(maxy, (ty + 1) << shift) - 1;
+        hit = vgx_tile_touched(h, x0, y0, x1, y1);
+      }
+      const u32 b = __ballot_sync(0xffffffffu, hit);
+      if(hit)
+        fn(pay, base + __popc(b & lt), tx, ty);
+      base += __popc(b);
+    }
+    if(lane == src)
+      mine = base;
+  }
+  return mine;
+}
+
 #endif

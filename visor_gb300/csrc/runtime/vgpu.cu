@@ -225,35 +225,54 @@ __global__ void k_scan_apply(const u32 *in, u32 *out, u32 n, const u32 *offsets,
 /* (tile, triangle) pairs in triangle order */
 __global__ void k_emit(VgxJob job, u32 rec_words, const u32 *offsets)
 {
+  /* no early exits: the warp walks big triangles together */
   const u32 tri = blockIdx.x * blockDim.x + threadIdx.x;
-  if(tri >= job.num_tris)
-    return;
-  const u32 n = offsets[tri + 1] - offsets[tri];
-  if(n == 0)
-    return;
+  const int lane = (int)(threadIdx.x & 31);
   const u32 total = offsets[job.num_tris];
-  if(total > job.pair_capacity)
-    return;
-  /* records start on 16-byte boundaries (whole uint4 words) */
-  const uint4 *r = (const uint4 *)((const u32 *)job.records + (u64)tri * rec_words);
-  int head[VGX_REC_HEAD];
-#pragma unroll
-  for(int i = 0; i < VGX_REC_HEAD / 4; i++)
+  bool active = tri < job.num_tris && total <= job.pair_capacity;
+  u32 off = 0;
+  if(active)
   {
-    const uint4 v = __ldg(r + i);
-    head[4 * i] = (int)v.x;
-    head[4 * i + 1] = (int)v.y;
-    head[4 * i + 2] = (int)v.z;
-    head[4 * i + 3] = (int)v.w;
+    off = offsets[tri];
+    active = offsets[tri + 1] != off;
   }
-  const VgxDraw *draws = (const VgxDraw *)job.draws;
-  const VgxTarget *targets = (const VgxTarget *)job.targets;
-  const VgxTarget &T = targets[draws[head[R_DRAW]].target];
+  int head[VGX_REC_HEAD];
+  u32 tile_base = 0, tiles_x = 0;
+  if(active)
+  {
+    /* records start on 16-byte boundaries (whole uint4 words) */
+    const uint4 *r = (const uint4 *)((const u32 *)job.records + (u64)tri * rec_words);
+#pragma unroll
+    for(int i = 0; i < VGX_REC_HEAD / 4; i++)
+    {
+      const uint4 v = __ldg(r + i);
+      head[4 * i] = (int)v.x;
+      head[4 * i + 1] = (int)v.y;
+      head[4 * i + 2] = (int)v.z;
+      head[4 * i + 3] = (int)v.w;
+    }
+    const VgxDraw *draws = (const VgxDraw *)job.draws;
+    const VgxTarget &T = ((const VgxTarget *)job.targets)[draws[head[R_DRAW]].target];
+    tile_base = T.tile_base;
+    tiles_x = T.tiles_x;
+  }
+  else
+  {
+#pragma unroll
+    for(int i = 0; i < VGX_REC_HEAD; i++)
+      head[i] = 0;
+  }
   u32 *keys = (u32 *)job.keys, *vals = (u32 *)job.vals;
-  const u32 off = offsets[tri];
-  vgx_visit_tiles(head, job.tile_shift, [&](u32 i, int tx, int ty) {
-    keys[off + i] = T.tile_base + (u32)ty * T.tiles_x + (u32)tx;
-    vals[off + i] = tri;
+  const bool big = active && vgx_bbox_tiles(head, job.tile_shift) > VGX_COOP_TILES;
+  if(active && !big)
+    vgx_visit_tiles(head, job.tile_shift, [&](u32 i, int tx, int ty) {
+      keys[off + i] = tile_base + (u32)ty * tiles_x + (u32)tx;
+      vals[off + i] = tri;
+    });
+  const u32 pay[4] = {off, tile_base, tiles_x, tri};
+  vgx_coop_visit_tiles(head, big, job.tile_shift, lane, pay, [&](const u32 *p, u32 i, int tx, int ty) {
+    keys[p[0] + i] = p[1] + (u32)ty * p[2] + (u32)tx;
+    vals[p[0] + i] = p[3];
   });
 }
 
