@@ -52,6 +52,12 @@ def test_translated_shaders_compile_for_sm103a(shader):
     assert vg.nvrtc_check(src) > 10000
 
 
+@pytest.mark.parametrize("shift,warps,deferred,blocks", [(4, 4, 0, 0), (4, 4, 2, 0), (3, 1, 1, 1), (5, 8, 0, 1)])
+def test_raster_variants_compile_for_sm103a(shift, warps, deferred, blocks):
+    src = vg.translate(vg.spirv(vs.SHADER_LAMBERT_TEX, 0), vg.spirv(vs.SHADER_LAMBERT_TEX, 4))
+    assert vg.nvrtc_check(src, shift, warps, deferred, blocks) > 10000
+
+
 def test_translator_rejects_garbage():
     with pytest.raises(ValueError):
         vg.translate([1, 2, 3, 4, 5, 6], vg.spirv(vs.SHADER_COLOR, 4))

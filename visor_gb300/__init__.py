@@ -126,12 +126,16 @@ def translate(vs_words, fs_words):
     return out.value.decode()
 
 
-def nvrtc_check(source, tile_shift=3, warps=1):
-    """NVRTC-compile translated source with the stage kernels for sm_103a; returns cubin bytes."""
+def nvrtc_check(source, tile_shift=3, warps=1, deferred=0, blocks=0):
+    """NVRTC-compile translated source with the stage kernels for sm_103a; returns cubin bytes.
+
+    deferred (0..2) and blocks (block-compressed textures) select the raster
+    variants the runtime builds for such jobs."""
     L = lib()
     log = C.create_string_buffer(65536)
     nbytes = C.c_uint64(0)
-    rc = L.vgpu_program_check(source.encode(), tile_shift | (warps << 8), log, 65536, C.byref(nbytes))
+    key = tile_shift | (warps << 8) | (deferred << 16) | ((1 if blocks else 0) << 18)
+    rc = L.vgpu_program_check(source.encode(), key, log, 65536, C.byref(nbytes))
     if rc != 0:
         raise RuntimeError("NVRTC failed:\n" + log.value.decode())
     return int(nbytes.value)

@@ -299,12 +299,17 @@ __global__ void k_radix_hist(const u32 *keys, u32 n, const u32 *n_dev, u32 shift
   h[threadIdx.x] = 0;
   __syncthreads();
   u32 base = blockIdx.x * kSortTile;
+  u32 rk[kSortItems];
+#pragma unroll
   for(int i = 0; i < kSortItems; i++)
   {
-    u32 idx = base + i * kSortBlock + threadIdx.x;
-    if(idx < n)
-      atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    const u32 idx = base + i * kSortBlock + threadIdx.x;
+    rk[i] = idx < n ? __ldg(keys + idx) : 0xffffffffu;
   }
+#pragma unroll
+  for(int i = 0; i < kSortItems; i++)
+    if(base + i * kSortBlock + threadIdx.x < n)
+      atomicAdd(&h[(rk[i] >> shift) & 255u], 1u);
   __syncthreads();
   hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
@@ -320,6 +325,16 @@ __global__ void k_radix_scatter(const u32 *keys, const u32 *vals, u32 n, const u
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   base_d[threadIdx.x] = hist_scanned[threadIdx.x * nblocks + blockIdx.x];
   const u32 lt = (1u << lane) - 1u;
+  /* every round's key and value are loaded up front so the loads overlap */
+  u32 rk[kSortItems], rv[kSortItems];
+#pragma unroll
+  for(int round = 0; round < kSortItems; round++)
+  {
+    const u32 idx = blockIdx.x * kSortTile + round * kSortBlock + threadIdx.x;
+    rk[round] = idx < n ? __ldg(keys + idx) : 0u;
+    rv[round] = idx < n ? __ldg(vals + idx) : 0u;
+  }
+#pragma unroll
   for(int round = 0; round < kSortItems; round++)
   {
     for(int k = threadIdx.x; k < (kSortBlock / 32) * 256; k += kSortBlock)
@@ -327,7 +342,7 @@ __global__ void k_radix_scatter(const u32 *keys, const u32 *vals, u32 n, const u
     __syncthreads();
     const u32 idx = blockIdx.x * kSortTile + round * kSortBlock + threadIdx.x;
     const bool valid = idx < n;
-    const u32 key = valid ? keys[idx] : 0u;
+    const u32 key = rk[round];
     const u32 dig = (key >> shift) & 255u;
     const u32 peers = __match_any_sync(0xffffffffu, valid ? dig : 256u + lane);
     const u32 rank = __popc(peers & lt);
@@ -349,7 +364,7 @@ __global__ void k_radix_scatter(const u32 *keys, const u32 *vals, u32 n, const u
     {
       const u32 pos = base_d[dig] + wcnt[w][dig] + rank;
       okeys[pos] = key;
-      ovals[pos] = vals[idx];
+      ovals[pos] = rv[round];
     }
     __syncthreads();
     base_d[threadIdx.x] += tot[threadIdx.x];
