@@ -36,6 +36,13 @@
 #ifndef VGX_DEFERRED
 #define VGX_DEFERRED 0
 #endif
+/* Coverage rows of a batch: 1 classifies each triangle's clipped rectangle by its
+   corners (fully covered, empty or partly covered) and spreads the partly covered
+   rows over the warp; 0 lets each lane walk its own rows, cheaper for jobs of
+   mostly tiny triangles (those with more triangles than pixels, VGX_DEFERRED 2). */
+#ifndef VGX_ROW_SPREAD
+#define VGX_ROW_SPREAD (VGX_DEFERRED != 2)
+#endif
 #if VGX_DEFERRED == 2
 #define VGX_REC VGX_REC_HEAD
 #else
@@ -242,6 +249,8 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
                    (D.blend_enable ? S_BLEND : 0u) | ((D.src_factor & 31u) << 5) |
                    ((D.dst_factor & 31u) << 10) | (depth_test ? S_DEPTH_TEST : 0u) |
                    ((D.blend_op & 7u) << 16);
+          if(vgx_span_safe(r))
+            st |= S_EXACT;
           r[R_STATE] = (int)st;
           u32 *rec = (u32 *)job.records + (u64)tri * VGX_REC;
 #pragma unroll
@@ -431,9 +440,20 @@ __device__ __forceinline__ float vgx_plane_depth(const VgxPlane &p, int dx, int 
 struct VgxWarpShared
 {
   uint4 pe[32], pa[32], pb[32], pd[32];
-  float4 col[32];
-  u32 frag[32]; /* deferred window: triangle record */
-  u32 fown[32]; /* deferred window: owner lane | pixel-half << 5 */
+  union
+  {
+    float4 col[32];
+    u16 item[256]; /* coverage rows to test: triangle << 11 | column mask << 3 | row */
+  };
+  union
+  {
+    struct
+    {
+      u32 frag[32]; /* deferred window: triangle record */
+      u32 fown[32]; /* deferred window: owner lane | pixel-half << 5 */
+    };
+    u64 rowm[32]; /* per triangle of the batch: its coverage rows, one byte each */
+  };
 #if !VGX_DEFERRED
   /* fragment queue: passing fragments wait here across batches until 32 can be
      shaded at once; in queue order, so each pixel's fragments stay in primitive order */
@@ -557,6 +577,8 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
   u32 mlo = 0, mhi = 0, st = 0;
   float dlo = 0.0f, dhi = 0.0f;
   bool finite = false;
+  u64 direct = 0;         /* coverage rows known without pixel tests */
+  u32 prows = 0, pitem = 0; /* rows to test pixel by pixel: count, first row | column mask << 3 */
   if((u32)lane < n)
   {
     const int v0x = r[R_V0X], v0y = r[R_V0Y], ABx = r[R_ABX], ABy = r[R_ABY];
@@ -577,6 +599,95 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     sh.pb[lane] = make_uint4((u32)b0, (u32)b1, (u32)b2, rec_index);
     sh.pd[lane] = make_uint4((u32)r[R_DEPTH], (u32)r[R_DEPTH + 1], (u32)r[R_DEPTH + 2],
                              area < (1 << 22) ? PF_SMALL : 0u);
+#if VGX_ROW_SPREAD
+    /* coverage of the sub-tile, clipped to the bbox [min, max) (rasterizer.cpp:538-549) */
+    const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
+    const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
+    const int cx0 = max(minx - x0, 0), cx1 = min(maxx - x0, 8);
+    const int ry0 = max(miny - y0, 0), ry1 = min(maxy - y0, 8);
+    const bool exact = (st & S_EXACT) != 0;
+    const float d0 = __int_as_float(r[R_DEPTH]), d1 = __int_as_float(r[R_DEPTH + 1]),
+                d2 = __int_as_float(r[R_DEPTH + 2]);
+    /* depth bounds need true barycentrics (convex weights, affine in the pixel) */
+    finite = exact && isfinite(d0) && isfinite(d1) && isfinite(d2);
+    const float mag = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
+    const float margin = mag * 2.0e-6f + 1.0e-30f; /* > the rounding of pixdepth (~4e-7 relative) */
+    dlo = fminf(d0, fminf(d1, d2)) - margin;
+    dhi = fmaxf(d0, fmaxf(d1, d2)) + margin;
+    if(cx0 < cx1 && ry0 < ry1)
+    {
+      const u32 colmask = (0xffu >> (8 - cx1)) & (0xffu << cx0);
+      /* edge values at the clipped rectangle's corners */
+      int ce[4][3];
+#pragma unroll
+      for(int c = 0; c < 4; c++)
+      {
+        const int dx = (c & 1) ? cx1 - 1 : cx0, dy = (c & 2) ? ry1 - 1 : ry0;
+        ce[c][0] = e0 + a0 * dx + b0 * dy;
+        ce[c][1] = e1 + a1 * dx + b1 * dy;
+        ce[c][2] = e2 + a2 * dx + b2 * dy;
+      }
+      /* rectangles are classified by their corners only where some lane's is
+         taller than 3 rows (short ones are walked row by row) */
+      if(__any_sync(__activemask(), ry1 - ry0 > 3))
+      {
+        bool empty = false, full = true;
+#pragma unroll
+        for(int k = 0; k < 3; k++)
+        {
+          const int lo = min(min(ce[0][k], ce[1][k]), min(ce[2][k], ce[3][k]));
+          const int hi = max(max(ce[0][k], ce[1][k]), max(ce[2][k], ce[3][k]));
+          empty |= hi < 0;
+          full &= lo >= 0;
+        }
+        if(exact && full)
+        {
+          /* every pixel of the rectangle is covered */
+          const u64 rows = (~0ull >> (64 - 8 * (ry1 - ry0))) << (8 * ry0);
+          direct = ((u64)colmask * 0x0101010101010101ull) & rows;
+        }
+        else if(!(exact && empty))
+        {
+          /* rows the warp evaluates pixel by pixel below */
+          prows = (u32)(ry1 - ry0);
+          pitem = (u32)ry0 | (colmask << 3);
+        }
+      }
+      else
+      {
+        prows = (u32)(ry1 - ry0);
+        pitem = (u32)ry0 | (colmask << 3);
+      }
+      if(finite)
+      {
+        /* Tighter bound over this sub-tile: with exact barycentrics the depth is affine
+           in (x, y), so over the covered part of the clipped rectangle it lies between
+           its values at the rectangle's corners.  Each corner value is computed like a
+           pixel's and widened by its own rounding bound (1e-6 of the sum of the terms'
+           magnitudes, which grows outside the triangle), the pixels' rounding by margin. */
+        const float ia = __int_as_float(r[R_INVAREA]);
+        float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+#pragma unroll
+        for(int c = 0; c < 4; c++)
+        {
+          const float n0 = (float)ce[c][0] * ia;
+          const float n1 = (float)ce[c][1] * ia;
+          const float n2 = (float)ce[c][2] * ia;
+          const float t0 = n0 * d0, t1 = n1 * d1, t2 = n2 * d2;
+          const float z = t0 + t1 + t2;
+          const float w = (fabsf(t0) + fabsf(t1) + fabsf(t2)) * 1.0e-6f;
+          lo = fminf(lo, z - w);
+          hi = fmaxf(hi, z + w);
+        }
+        if(isfinite(lo) && isfinite(hi))
+        {
+          dlo = fmaxf(dlo, lo - margin);
+          dhi = fminf(dhi, hi + margin);
+        }
+      }
+    }
+  }
+#else
     /* coverage of the sub-tile, clipped to the bbox [min, max) (rasterizer.cpp:538-549) */
     const int minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
     const int maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
@@ -608,7 +719,8 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     }
     const float d0 = __int_as_float(r[R_DEPTH]), d1 = __int_as_float(r[R_DEPTH + 1]),
                 d2 = __int_as_float(r[R_DEPTH + 2]);
-    finite = isfinite(d0) && isfinite(d1) && isfinite(d2);
+    /* depth bounds need true barycentrics (convex weights, affine in the pixel) */
+    finite = ((u32)r[R_STATE] & S_EXACT) && isfinite(d0) && isfinite(d1) && isfinite(d2);
     const float mag = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
     const float margin = mag * 2.0e-6f + 1.0e-30f; /* > the rounding of pixdepth (~4e-7 relative) */
     dlo = fminf(d0, fminf(d1, d2)) - margin;
@@ -642,6 +754,93 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
       }
     }
   }
+#endif
+  /* Rows of partly covered rectangles (and of triangles without exact corner
+     arithmetic) are tested pixel by pixel: each row is walked from dx = 7 down to
+     0, shifting each pixel's inside bit (all three edge values non-negative) in at
+     bit 0.  A lane walks its own triangle's rows when the longest such run is short
+     (divergent lanes cost the warp the longest run); otherwise the (triangle, row)
+     items are spread over the warp, 32 at a time. */
+#if VGX_ROW_SPREAD
+  {
+    u32 incl = prows;
+#pragma unroll
+    for(int o = 1; o < 32; o <<= 1)
+    {
+      const u32 v = __shfl_up_sync(0xffffffffu, incl, o);
+      if(lane >= o)
+        incl += v;
+    }
+    const u32 items = __shfl_sync(0xffffffffu, incl, 31);
+    const u32 longest = __reduce_max_sync(0xffffffffu, prows);
+    if(((items + 31u) >> 5) * 5u + 4u >= longest * 4u)
+    {
+      mlo = (u32)direct;
+      mhi = (u32)(direct >> 32);
+      if(prows)
+      {
+        const uint4 pe = sh.pe[lane], pa = sh.pa[lane], pb = sh.pb[lane];
+        const int a0 = (int)pa.x, a1 = (int)pa.y, a2 = (int)pa.z;
+        const u32 cm = (pitem >> 3) & 0xffu;
+        for(u32 dy = pitem & 7u; dy < (pitem & 7u) + prows; dy++)
+        {
+          int q0 = (int)pe.x + (int)pb.x * (int)dy + 7 * a0;
+          int q1 = (int)pe.y + (int)pb.y * (int)dy + 7 * a1;
+          int q2 = (int)pe.z + (int)pb.z * (int)dy + 7 * a2;
+          u32 row = 0;
+#pragma unroll
+          for(int dx = 7; dx >= 0; dx--)
+          {
+            row = __funnelshift_l(~(u32)(q0 | q1 | q2), row, 1);
+            q0 -= a0;
+            q1 -= a1;
+            q2 -= a2;
+          }
+          row &= cm;
+          if(dy < 4)
+            mlo |= row << (dy * 8);
+          else
+            mhi |= row << ((dy - 4) * 8);
+        }
+      }
+    }
+    else
+    {
+      __syncwarp(); /* the arrays alias the shading window, read by other lanes before */
+      sh.rowm[lane] = direct;
+      for(u32 j = 0; j < prows; j++)
+        sh.item[incl - prows + j] = (u16)(((u32)lane << 11) | (pitem + j));
+      __syncwarp();
+      for(u32 base = 0; base < items; base += 32)
+      {
+        if(base + (u32)lane < items)
+        {
+          const u32 it = sh.item[base + lane];
+          const u32 t = it >> 11, dy = it & 7u, cm = (it >> 3) & 0xffu;
+          const uint4 pe = sh.pe[t], pa = sh.pa[t], pb = sh.pb[t];
+          const int a0 = (int)pa.x, a1 = (int)pa.y, a2 = (int)pa.z;
+          int q0 = (int)pe.x + (int)pb.x * (int)dy + 7 * a0;
+          int q1 = (int)pe.y + (int)pb.y * (int)dy + 7 * a1;
+          int q2 = (int)pe.z + (int)pb.z * (int)dy + 7 * a2;
+          u32 row = 0;
+#pragma unroll
+          for(int dx = 7; dx >= 0; dx--)
+          {
+            row = __funnelshift_l(~(u32)(q0 | q1 | q2), row, 1);
+            q0 -= a0;
+            q1 -= a1;
+            q2 -= a2;
+          }
+          ((unsigned char *)sh.rowm)[t * 8 + dy] = (unsigned char)(row & cm);
+        }
+      }
+      __syncwarp();
+      const u64 m = sh.rowm[lane];
+      mlo = (u32)m;
+      mhi = (u32)(m >> 32);
+    }
+  }
+#endif
   covered_total += __popc(mlo) + __popc(mhi);
 
   /* conservative depth rejection of whole triangles against the sub-tile's depth range */

@@ -27,11 +27,32 @@
 #define R_STATE 19
 #define VGX_REC_HEAD 20
 
+/* state-word bit set by setup when the triangle's edge functions stay below 2^29
+   in magnitude over its bbox (vgx_span_safe): their 32-bit evaluation never wraps
+   there, so they are exact affine functions of the pixel and their extremes over
+   a rectangle lie on its corners */
+#define S_EXACT (1u << 19)
+
+__device__ __forceinline__ bool vgx_span_safe(const int *r)
+{
+  const long long minx = r[R_MIN] & 0xffff, miny = (int)((u32)r[R_MIN] >> 16);
+  const long long maxx = r[R_MAX] & 0xffff, maxy = (int)((u32)r[R_MAX] >> 16);
+  const long long v0x = r[R_V0X], v0y = r[R_V0Y];
+  const long long pax = max(llabs(v0x - minx), llabs(v0x - maxx));
+  const long long pay = max(llabs(v0y - miny), llabs(v0y - maxy));
+  const long long abx = llabs((long long)r[R_ABX]), aby = llabs((long long)r[R_ABY]);
+  const long long acx = llabs((long long)r[R_ACX]), acy = llabs((long long)r[R_ACY]);
+  const long long lim = 1ll << 29;
+  /* |ux|, |uy| < 2^29 and |area2| < 2^29 bound the third function by 3 * 2^29 */
+  return acx * pay + acy * pax < lim && pax * aby + pay * abx < lim && llabs((long long)r[R_AREA2]) < lim;
+}
+
 /* Conservative tile test: a tile can hold covered pixels only if every
    (barymul-signed) edge function is >= 0 at some corner of its pixel rectangle
-   [x0,x1]x[y0,y1] (inclusive).  The functions are affine, so their maxima lie
-   on corners; evaluation uses the integer arithmetic of the per-pixel test
-   (rasterizer.cpp:303-309), so no covered pixel is ever dropped. */
+   [x0,x1]x[y0,y1] (inclusive).  For an S_EXACT triangle the functions are
+   affine, so their maxima lie on corners; evaluation uses the integer
+   arithmetic of the per-pixel test (rasterizer.cpp:303-309), so no covered
+   pixel is ever dropped.  Other triangles touch every tile of their bbox. */
 __device__ __forceinline__ bool vgx_tile_touched(const int *r, int x0, int y0, int x1, int y1)
 {
   const int v0x = r[R_V0X], v0y = r[R_V0Y], ABx = r[R_ABX], ABy = r[R_ABY], ACx = r[R_ACX],
@@ -70,7 +91,7 @@ __device__ __forceinline__ u32 vgx_visit_tiles(const int *r, u32 shift, F fn)
       {
         const int x0 = max(minx, tx << shift), x1 = min(maxx, (tx + 1) << shift) - 1;
         const int y0 = max(miny, ty << shift), y1 = min(maxy, (ty + 1) << shift) - 1;
-        hit = vgx_tile_touched(r, x0, y0, x1, y1);
+        hit = !((u32)r[R_STATE] & S_EXACT) || vgx_tile_touched(r, x0, y0, x1, y1);
       }
       if(hit)
       {
@@ -115,6 +136,7 @@ __device__ __forceinline__ u32 vgx_coop_visit_tiles(const int *r, bool big, u32 
 #pragma unroll
     for(int i = 0; i < 10; i++)
       h[i] = __shfl_sync(0xffffffffu, r[i], src);
+    const bool exact = (__shfl_sync(0xffffffffu, (u32)r[R_STATE], src) & S_EXACT) != 0;
     u32 pay[4];
 #pragma unroll
     for(int i = 0; i < 4; i++)
@@ -136,7 +158,7 @@ __device__ __forceinline__ u32 vgx_coop_visit_tiles(const int *r, bool big, u32 
         ty = ty0 + (int)(i / bw);
         const int x0 = max(minx, tx << shift), x1 = min(maxx, (tx + 1) << shift) - 1;
         const int y0 = max(miny, ty << shift), y1 = min(maxy, (ty + 1) << shift) - 1;
-        hit = vgx_tile_touched(h, x0, y0, x1, y1);
+        hit = !exact || vgx_tile_touched(h, x0, y0, x1, y1);
       }
       const u32 b = __ballot_sync(0xffffffffu, hit);
       if(hit)

@@ -390,10 +390,21 @@ __global__ void k_ranges(const u32 *keys, const u32 *pair_total, u32 capacity, u
   const u32 n = *pair_total;
   if(n > capacity)
     return;
-  for(u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  const u32 lane = threadIdx.x & 31u;
+  /* the loop bound is uniform per warp: each warp appends its tile heads with one
+     atomic (heads of many small tiles would otherwise queue on one address) */
+  for(u32 i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x)
   {
-    const u32 k = keys[i];
-    if(i == 0 || keys[i - 1] != k)
+    const u32 i = i0 + threadIdx.x;
+    const bool in = i < n;
+    const u32 k = in ? keys[i] : 0u;
+    const bool head = in && (i == 0 || keys[i - 1] != k);
+    const u32 hb = __ballot_sync(0xffffffffu, head);
+    u32 wbase = 0;
+    if(lane == 0 && hb)
+      wbase = atomicAdd(&status[3], (u32)__popc(hb));
+    wbase = __shfl_sync(0xffffffffu, wbase, 0);
+    if(head)
     {
       tstart[k] = i;
       u32 lo = 0, hi = num_targets - 1;
@@ -405,9 +416,9 @@ __global__ void k_ranges(const u32 *keys, const u32 *pair_total, u32 capacity, u
         else
           hi = mid - 1;
       }
-      work[atomicAdd(&status[3], 1u)] = make_uint2(k, lo);
+      work[wbase + __popc(hb & ((1u << lane) - 1u))] = make_uint2(k, lo);
     }
-    if(i == n - 1 || keys[i + 1] != k)
+    if(in && (i == n - 1 || keys[i + 1] != k))
       tend[k] = i + 1;
   }
 }
@@ -424,13 +435,24 @@ __global__ void k_clear_empty(const VgxTarget *targets, u32 num_targets, u32 shi
       continue;
     const u32 W = (u32)T.width, H = (u32)T.height;
     const u32 qpr = (W + 3) >> 2;
-    const u32 nq = qpr * H;
     u32 *color = (u32 *)T.color;
     float *depth = (float *)T.depth;
-    for(u32 q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+    /* quad q = y * qpr + xq, advanced by the grid stride without dividing per quad */
+    const u32 stride = gridDim.x * blockDim.x;
+    const u32 sy = stride / qpr, sx = stride - sy * qpr;
+    const u32 q0 = blockIdx.x * blockDim.x + threadIdx.x;
+    u32 y = q0 / qpr, xq = q0 - y * qpr;
+    for(; y < H; y += sy, xq += sx)
     {
-      const u32 y = q / qpr, x = (q - y * qpr) << 2;
-      if(tend[T.tile_base + (y >> shift) * T.tiles_x + (x >> shift)])
+      if(xq >= qpr)
+      {
+        xq -= qpr;
+        y++;
+        if(y >= H)
+          break;
+      }
+      const u32 x = xq << 2;
+      if(__ldg(tend + T.tile_base + (y >> shift) * T.tiles_x + (x >> shift)))
         continue;
       const u64 pix = (u64)y * W + x;
       if(x + 4 <= W && (pix & 3) == 0)
