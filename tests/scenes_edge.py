@@ -101,6 +101,22 @@ def offscreen(lib):
     return _tri_scene(lib, 64, 64, tris, {})
 
 
+def guard_band(lib, blend=False):
+    """Triangles with vertices thousands of pixels off-screen: some exceed the bound
+    under which edge functions are evaluated from rectangle corners (their tiles and
+    depth bounds take the conservative path), mixed with ordinary ones."""
+    tris = [
+        [(-16000, -16000, 0.5, RED), (16000, -100, 0.5, RED), (-100, 16000, 0.5, RED)],
+        [(-9000, 30, 0.4, GREEN), (9000, 22, 0.6, GREEN), (40, 9000, 0.2, GREEN)],
+        [(10, 10, 0.3, BLUE), (50, 14, 0.3, BLUE), (20, 50, 0.3, BLUE)],
+        [(-15000, 70, 0.9, HALF), (70, -15000, 0.9, HALF), (15000, 15000, 0.9, HALF)],
+        [(-16000, -15000, 0.1, HALF), (16000, -14990, 0.1, HALF), (30, 40, 0.45, HALF)],
+    ]
+    kw = {"depth_op": vs.CMP_LEQUAL, "blend_enable": 1, "src_factor": vs.BLEND_SRC_ALPHA,
+          "dst_factor": vs.BLEND_ONE_MINUS_SRC_ALPHA} if blend else {}
+    return _tri_scene(lib, 64, 64, tris, kw)
+
+
 def strip(lib):
     verts = []
     for i in range(12):
@@ -271,6 +287,8 @@ EDGE_SCENES = {
     "blend_overlap": blend_overlap,
     "shared_edges": shared_edges,
     "offscreen": offscreen,
+    "guard_band": guard_band,
+    "guard_band_blend": lambda lib: guard_band(lib, blend=True),
     "strip": strip,
     "load_pass": load_pass,
     "texture_wrap": texture_wrap,
