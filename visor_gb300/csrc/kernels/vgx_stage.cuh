@@ -56,6 +56,9 @@
 #define VGX_SUB_EDGE (1 << (VGX_TILE_SHIFT - 3))
 #define VGX_SUBS (VGX_SUB_EDGE * VGX_SUB_EDGE)
 #define VGX_SUBS_PER_WARP ((VGX_SUBS + VGX_RASTER_WARPS - 1) / VGX_RASTER_WARPS)
+/* 1: each warp owns one 8x8 sub-tile of a larger bin and filters the bin's
+   triangles by bbox before batching them */
+#define VGX_SUB_FILTER (VGX_SUBS_PER_WARP == 1 && VGX_SUBS > 1)
 
 /* state word */
 #define S_DEPTH_OP(s) ((s)&7u)
@@ -440,6 +443,9 @@ __device__ __forceinline__ float vgx_plane_depth(const VgxPlane &p, int dx, int 
 struct VgxWarpShared
 {
   uint4 pe[32], pa[32], pb[32], pd[32];
+#if VGX_SUB_FILTER
+  u32 ring[64]; /* records whose bbox meets the warp's sub-tile, waiting for a batch */
+#endif
   union
   {
     float4 col[32];
@@ -1183,6 +1189,62 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
     for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
       any_valid |= valid[j];
     const u32 start = tstart[tile], end = tend[tile];
+#if VGX_SUB_FILTER
+    /* The warp's own 8x8 sub-tile is a quarter (or less) of the bin: triangles whose
+       bbox misses it are dropped before the batch, and the rest queue up (a ring of
+       64 record indices, in primitive order) until 32 fill a batch. */
+    {
+      const u32 lt = (1u << lane) - 1u;
+      u32 head = 0, cq = 0, base = start;
+      while(base < end || cq)
+      {
+        while(cq < 32 && base < end)
+        {
+          const u32 n = min(32u, end - base);
+          bool keep = false;
+          u32 ri = 0;
+          if((u32)lane < n)
+          {
+            ri = vals[base + lane];
+            const uint2 bb = __ldg((const uint2 *)((const u32 *)job.records + (u64)ri * VGX_REC + R_MIN));
+            const int minx = (int)(bb.x & 0xffffu), miny = (int)(bb.x >> 16);
+            const int maxx = (int)(bb.y & 0xffffu), maxy = (int)(bb.y >> 16);
+            keep = minx < sx[0] + 8 && maxx > sx[0] && miny < sy[0] + 8 && maxy > sy[0];
+          }
+          const u32 kb = __ballot_sync(0xffffffffu, keep);
+          if(keep)
+            sh.ring[(head + cq + __popc(kb & lt)) & 63u] = ri;
+          cq += __popc(kb);
+          base += n;
+        }
+        __syncwarp();
+        const u32 nb = min(32u, cq);
+        int r[VGX_REC_HEAD];
+        u32 rec_index = 0;
+        if((u32)lane < nb)
+        {
+          rec_index = sh.ring[(head + lane) & 63u];
+          const u32 *g = (const u32 *)job.records + (u64)rec_index * VGX_REC;
+#pragma unroll
+          for(int q = 0; q < VGX_REC_HEAD; q += 4)
+          {
+            const uint4 v = __ldg((const uint4 *)(g + q));
+            r[q] = (int)v.x;
+            r[q + 1] = (int)v.y;
+            r[q + 2] = (int)v.z;
+            r[q + 3] = (int)v.w;
+          }
+        }
+        const bool last = base >= end && cq <= 32;
+        vgx_subtile_batch(job, sh, lane, nb, r, rec_index, sx[0], sy[0], in[0], col[0], dep[0], vis[0],
+                          qn, last, covered_total, shaded_total, tested_total);
+        head += nb;
+        cq -= nb;
+        if(last)
+          break;
+      }
+    }
+#else
     for(u32 base = start; any_valid && base < end; base += 32)
     {
       const u32 n = min(32u, end - base);
@@ -1209,6 +1271,7 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
                             vis[j], qn, base + 32 >= end, covered_total, shaded_total,
                             tested_total);
     }
+#endif
 #if VGX_DEFERRED
 #pragma unroll
     for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
