@@ -1045,23 +1045,34 @@ __device__ __forceinline__ void vgx_shade_deferred(const VgxJob &job, VgxWarpSha
       const u32 rec = sh.frag[lane], own = sh.fown[lane];
       const int px = x0 + (int)(own & 7), py = y0 + (int)((own >> 3) & 3) + 4 * (int)(own >> 5);
       const u32 *g = (const u32 *)job.records + (u64)rec * VGX_REC;
+      /* the record header as 16-byte loads (records are 16-byte aligned) */
+      u32 h[VGX_REC_HEAD];
+#pragma unroll
+      for(int q = 0; q < VGX_REC_HEAD; q += 4)
+      {
+        const uint4 v = __ldg((const uint4 *)(g + q));
+        h[q] = v.x;
+        h[q + 1] = v.y;
+        h[q + 2] = v.z;
+        h[q + 3] = v.w;
+      }
       int b0, b1, b2;
-      vgx_bary(g, px, py, b0, b1, b2);
-      const float ia = __uint_as_float(__ldg(g + R_INVAREA));
+      vgx_bary(h, px, py, b0, b1, b2);
+      const float ia = __uint_as_float(h[R_INVAREA]);
       float nb[4];
       nb[0] = (float)b0 * ia;
       nb[1] = (float)b1 * ia;
       nb[2] = (float)b2 * ia;
       /* perspective correction, rasterizer.cpp:580-588 */
-      nb[0] = nb[0] * __uint_as_float(__ldg(g + R_INVW));
-      nb[1] = nb[1] * __uint_as_float(__ldg(g + R_INVW + 1));
-      nb[2] = nb[2] * __uint_as_float(__ldg(g + R_INVW + 2));
+      nb[0] = nb[0] * __uint_as_float(h[R_INVW]);
+      nb[1] = nb[1] * __uint_as_float(h[R_INVW + 1]);
+      nb[2] = nb[2] * __uint_as_float(h[R_INVW + 2]);
       const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
       nb[0] = nb[0] * invlen;
       nb[1] = nb[1] * invlen;
       nb[2] = nb[2] * invlen;
       nb[3] = 0.0f;
-      const VgxDraw &D = draws[__ldg(g + R_DRAW)];
+      const VgxDraw &D = draws[h[R_DRAW]];
       float iv[3][VGX_K > 0 ? VGX_K : 1];
 #if VGX_DEFERRED == 2
       /* the vertex shader again for the triangle's three vertices (deterministic, so
@@ -1075,13 +1086,26 @@ __device__ __forceinline__ void vgx_shade_deferred(const VgxJob &job, VgxWarpSha
         vgx_vs(D, vidx[v], pos, iv[v]);
       }
 #else
+      {
+        /* the interpolants as 16-byte loads (a record is padded to a multiple of 4 words) */
+        float w[(3 * VGX_K + 3) & ~3];
 #pragma unroll
-      for(int v = 0; v < 3; v++)
+        for(int q = 0; q < 3 * VGX_K; q += 4)
+        {
+          const uint4 v = __ldg((const uint4 *)(g + VGX_REC_HEAD + q));
+          w[q] = __uint_as_float(v.x);
+          w[q + 1] = __uint_as_float(v.y);
+          w[q + 2] = __uint_as_float(v.z);
+          w[q + 3] = __uint_as_float(v.w);
+        }
 #pragma unroll
-        for(int q = 0; q < VGX_K; q++)
-          iv[v][q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + v * VGX_K + q));
+        for(int v = 0; v < 3; v++)
+#pragma unroll
+          for(int q = 0; q < VGX_K; q++)
+            iv[v][q] = w[v * VGX_K + q];
+      }
 #endif
-      sh.col[lane] = vgx_fs(D, nb, iv[0], iv[1], iv[2], __uint_as_float(__ldg(g + R_LOD)));
+      sh.col[lane] = vgx_fs(D, nb, iv[0], iv[1], iv[2], __uint_as_float(h[R_LOD]));
     }
     __syncwarp();
     k = excl;
