@@ -117,6 +117,18 @@ def guard_band(lib, blend=False):
     return _tri_scene(lib, 64, 64, tris, kw)
 
 
+def corner_sliver(lib):
+    """Triangles whose vertices lie a thousand pixels off-screen: the bbox clamped to
+    the target spans every bin tile while the covered corner lies in one."""
+    tris = [
+        [(-1000, 1006, 0.5, RED), (1006, -1000, 0.5, RED), (-1000, -1000, 0.5, RED)],
+        [(1060, -940, 0.4, GREEN), (-940, 1060, 0.4, GREEN), (1060, 1060, 0.4, GREEN)],
+        [(-1000, 40, 0.3, BLUE), (1000, 41, 0.3, BLUE), (-1000, 43, 0.3, BLUE)],
+        [(10, 10, 0.6, HALF), (50, 12, 0.6, HALF), (30, 50, 0.6, HALF)],
+    ]
+    return _tri_scene(lib, 64, 64, tris, {})
+
+
 def strip(lib):
     verts = []
     for i in range(12):
@@ -288,6 +300,7 @@ EDGE_SCENES = {
     "shared_edges": shared_edges,
     "offscreen": offscreen,
     "guard_band": guard_band,
+    "corner_sliver": corner_sliver,
     "guard_band_blend": lambda lib: guard_band(lib, blend=True),
     "strip": strip,
     "load_pass": load_pass,

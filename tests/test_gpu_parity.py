@@ -67,7 +67,8 @@ def test_gpu_matches_oracle(device, oracle, name, mode):
     assert gk == ref["counters"]
 
 
-VARIANT_SCENES = ["blend_overlap", "depth_lequal", "offscreen", "guard_band", "guard_band_blend", "strip",
+VARIANT_SCENES = ["blend_overlap", "depth_lequal", "offscreen", "guard_band", "guard_band_blend", "corner_sliver",
+                  "strip",
                   "texture_wrap", "load_pass",
                   "cfg1_sphere", "cfg2_small_blend", "cfg3_small_trilinear", "cfg4_small"]
 

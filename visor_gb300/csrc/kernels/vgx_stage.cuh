@@ -140,7 +140,7 @@ __device__ __forceinline__ bool vgx_tri_indices(const VgxDraw &D, u32 local, u32
   return bad;
 }
 
-extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
+extern "C" __global__ void __launch_bounds__(256, 4) vgx_setup(VgxJob job)
 {
   __shared__ u32 s_draw;
   const VgxDraw *draws = (const VgxDraw *)job.draws;
@@ -156,7 +156,7 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
   u32 keep = 0, tested = 0;
   int r[VGX_REC_HEAD] = {0}; /* the triangle's record header when has_rec */
   bool has_rec = false;
-  u32 ntiles = 0;
+  u32 ntiles = 0, tbase = 0, tcols = 0;
   if(live)
   {
     u32 di = s_draw;
@@ -164,6 +164,8 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
       di++;
     const VgxDraw &D = draws[di];
     const VgxTarget T = ((const VgxTarget *)job.targets)[D.target];
+    tbase = T.tile_base;
+    tcols = T.tiles_x;
     const u32 local = tri - D.tri_base;
     u32 vidx[3];
     const bool bad = vgx_tri_indices(D, local, vidx);
@@ -273,10 +275,27 @@ extern "C" __global__ void __launch_bounds__(256) vgx_setup(VgxJob job)
   /* tiles touched: a thread walks a small triangle's tiles, the warp a big one's */
   const bool big = has_rec && vgx_bbox_tiles(r, VGX_TILE_SHIFT) > VGX_COOP_TILES;
   if(has_rec && !big)
-    ntiles = vgx_count_tiles(r);
-  const u32 none[4] = {0u, 0u, 0u, 0u};
-  const u32 coop = vgx_coop_visit_tiles(r, big, VGX_TILE_SHIFT, (int)(threadIdx.x & 31), none,
-                                        [](const u32 *, u32, int, int) {});
+  {
+    int ftx = 0, fty = 0;
+    ntiles = vgx_visit_tiles(r, VGX_TILE_SHIFT, [&](u32 i, int tx, int ty) {
+      if(i == 0)
+      {
+        ftx = tx;
+        fty = ty;
+      }
+    });
+    /* a triangle in one bin tile is emitted from this key without its record */
+    if(ntiles == 1 && job.first_keys)
+      ((u32 *)job.first_keys)[tri] = tbase + (u32)fty * tcols + (u32)ftx;
+  }
+  /* a big bbox can still touch a single tile (a triangle mostly off-screen): the
+     first tile's key is left for every triangle the warp walks */
+  const u32 pay[4] = {tri, tbase, tcols, job.first_keys ? 1u : 0u};
+  const u32 coop = vgx_coop_visit_tiles(r, big, VGX_TILE_SHIFT, (int)(threadIdx.x & 31), pay,
+                                        [&](const u32 *p, u32 i, int tx, int ty) {
+                                          if(i == 0 && p[3])
+                                            ((u32 *)job.first_keys)[p[0]] = p[1] + (u32)ty * p[2] + (u32)tx;
+                                        });
   if(big)
     ntiles = coop;
   if(live)

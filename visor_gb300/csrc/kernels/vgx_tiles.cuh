@@ -19,13 +19,15 @@
 #define R_BARYMUL 7
 #define R_MIN 8
 #define R_MAX 9
-#define R_INVAREA 10
-#define R_DEPTH 11
-#define R_INVW 14
-#define R_DRAW 17
-#define R_LOD 18
-#define R_STATE 19
+#define R_DRAW 10  /* words 0..11 (48 bytes) hold what binning reads */
+#define R_STATE 11
+#define R_INVAREA 12
+#define R_DEPTH 13
+#define R_INVW 16
+#define R_LOD 19
 #define VGX_REC_HEAD 20
+/* words of the header the binning kernels read (bbox, edges, draw, state) */
+#define VGX_REC_BIN 12
 
 /* state-word bit set by setup when the triangle's edge functions stay below 2^29
    in magnitude over its bbox (vgx_span_safe): their 32-bit evaluation never wraps

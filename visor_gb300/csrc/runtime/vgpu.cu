@@ -229,21 +229,34 @@ __global__ void k_emit(VgxJob job, u32 rec_words, const u32 *offsets)
   const u32 tri = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = (int)(threadIdx.x & 31);
   const u32 total = offsets[job.num_tris];
+  u32 *keys = (u32 *)job.keys, *vals = (u32 *)job.vals;
   bool active = tri < job.num_tris && total <= job.pair_capacity;
   u32 off = 0;
   if(active)
   {
     off = offsets[tri];
-    active = offsets[tri + 1] != off;
+    const u32 n = offsets[tri + 1] - off;
+    active = n != 0;
+    if(n == 1 && job.first_keys)
+    {
+      /* one bin tile: setup left its key */
+      keys[off] = ((const u32 *)job.first_keys)[tri];
+      vals[off] = tri;
+      active = false;
+    }
   }
   int head[VGX_REC_HEAD];
   u32 tile_base = 0, tiles_x = 0;
+#pragma unroll
+  for(int i = VGX_REC_BIN; i < VGX_REC_HEAD; i++)
+    head[i] = 0;
   if(active)
   {
-    /* records start on 16-byte boundaries (whole uint4 words) */
+    /* records start on 16-byte boundaries (whole uint4 words); binning needs the
+       first VGX_REC_BIN words only */
     const uint4 *r = (const uint4 *)((const u32 *)job.records + (u64)tri * rec_words);
 #pragma unroll
-    for(int i = 0; i < VGX_REC_HEAD / 4; i++)
+    for(int i = 0; i < VGX_REC_BIN / 4; i++)
     {
       const uint4 v = __ldg(r + i);
       head[4 * i] = (int)v.x;
@@ -259,10 +272,9 @@ __global__ void k_emit(VgxJob job, u32 rec_words, const u32 *offsets)
   else
   {
 #pragma unroll
-    for(int i = 0; i < VGX_REC_HEAD; i++)
+    for(int i = 0; i < VGX_REC_BIN; i++)
       head[i] = 0;
   }
-  u32 *keys = (u32 *)job.keys, *vals = (u32 *)job.vals;
   const bool big = active && vgx_bbox_tiles(head, job.tile_shift) > VGX_COOP_TILES;
   if(active && !big)
     vgx_visit_tiles(head, job.tile_shift, [&](u32 i, int tx, int ty) {
@@ -940,6 +952,7 @@ struct Job
   std::vector<VgxTarget> targets;
   std::vector<u64> target_keys; /* colour address identifies a target */
   u32 num_tris = 0, num_tiles = 0, key_bits = 1, all_tiles = 0, all_opaque = 1;
+  u64 first_off = 0; /* word offset of the per-triangle first bin keys in the count arena */
   /* device */
   VgxDraw *d_draws = nullptr;
   VgxTarget *d_targets = nullptr;
@@ -1286,6 +1299,8 @@ static int list_build(vgpu_list *l)
       j.scan_levels.push_back(cnt_words);
       cnt_words += n + 1;
     }
+    j.first_off = cnt_words;
+    cnt_words += j.num_tris;
     int rc = list_dev_alloc(l, (void **)&j.d_draws,
                             std::max<size_t>(1, j.draws.size()) * sizeof(VgxDraw));
     if(!rc)
@@ -1509,6 +1524,7 @@ static VgxJob make_job(vgpu_queue *q, vgpu_list *l, Job &j, size_t ji)
   J.targets = (u64)j.d_targets;
   J.records = (u64)(l->d_records + j.rec_off);
   J.counts = (u64)(l->d_counts + j.cnt_off);
+  J.first_keys = (u64)(l->d_counts + j.first_off);
   J.keys = (u64)q->keys[0];
   J.vals = (u64)q->vals[0];
   J.keys_alt = (u64)q->keys[1];
