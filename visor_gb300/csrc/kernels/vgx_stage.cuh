@@ -145,10 +145,12 @@ extern "C" __global__ void __launch_bounds__(256, 4) vgx_setup(VgxJob job)
   __shared__ u32 s_draw;
   const VgxDraw *draws = (const VgxDraw *)job.draws;
   vgx_init_unorm8();
-  /* the block's triangles are consecutive: one search for the first one's draw,
-     then each thread steps forward over the (few) draws the block spans */
+  /* the block's triangles are consecutive: the first one's draw (from the table the
+     host builds with the job, else a search), then each thread steps forward over
+     the (few) draws the block spans */
   if(threadIdx.x == 0)
-    s_draw = vgx_find_draw(draws, job.num_draws, min(blockIdx.x * blockDim.x, job.num_tris - 1));
+    s_draw = job.block_draws ? ((const u32 *)job.block_draws)[blockIdx.x]
+                             : vgx_find_draw(draws, job.num_draws, min(blockIdx.x * blockDim.x, job.num_tris - 1));
   __syncthreads();
   const u32 tri = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = tri < job.num_tris;

@@ -137,6 +137,7 @@ typedef struct VgxJob {
   u64 counters;                       /* u64*: tris_out, tested, covered, shaded, depth-tested */
   u64 scratch;                        /* u32* scan/sort scratch */
   u64 first_keys;                     /* u32* per triangle: its bin tile, for triangles in one tile */
+  u64 block_draws;                    /* u32* per setup block of 256 triangles: the draw of its first */
   u32 num_draws, num_tris;
   u32 num_targets, num_tiles;
   u32 pair_capacity;

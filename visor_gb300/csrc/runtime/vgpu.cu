@@ -123,6 +123,7 @@ u32 g_tuning_gen = 1; /* bumped when a knob that shapes lists (bin tile, warps) 
 /* generic kernels                                                           */
 /* ------------------------------------------------------------------------ */
 
+constexpr u32 kSetupBlock = 256; /* vgx_setup's block: one thread per triangle */
 constexpr int kScanBlock = 256;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanBlock * kScanItems;
@@ -955,6 +956,8 @@ struct Job
   u64 first_off = 0; /* word offset of the per-triangle first bin keys in the count arena */
   /* device */
   VgxDraw *d_draws = nullptr;
+  std::vector<u32> block_draws; /* per setup block: the draw of its first triangle */
+  u32 *d_block_draws = nullptr;
   VgxTarget *d_targets = nullptr;
   u64 rec_off = 0, cnt_off = 0; /* word offsets into the list's record/count arenas */
   std::vector<u64> scan_levels; /* word offsets of scan scratch levels */
@@ -1031,6 +1034,7 @@ static void list_free_device(vgpu_list *l)
   for(Job &j : l->jobs)
   {
     list_dev_free(l, j.d_draws);
+    list_dev_free(l, j.d_block_draws);
     list_dev_free(l, j.d_targets);
   }
   list_dev_free(l, l->d_records);
@@ -1301,11 +1305,23 @@ static int list_build(vgpu_list *l)
     }
     j.first_off = cnt_words;
     cnt_words += j.num_tris;
+    /* the draw of each setup block's first triangle (draws are in tri_base order) */
+    std::vector<u32> &block_draws = j.block_draws;
+    block_draws.assign(std::max<u32>(1, (j.num_tris + kSetupBlock - 1) / kSetupBlock), 0u);
+    for(size_t b = 0, d = 0; b < block_draws.size(); b++)
+    {
+      const u32 t = (u32)std::min<u64>((u64)b * kSetupBlock, j.num_tris ? j.num_tris - 1 : 0);
+      while(d + 1 < j.draws.size() && j.draws[d + 1].tri_base <= t)
+        d++;
+      block_draws[b] = (u32)d;
+    }
     int rc = list_dev_alloc(l, (void **)&j.d_draws,
                             std::max<size_t>(1, j.draws.size()) * sizeof(VgxDraw));
     if(!rc)
       rc = list_dev_alloc(l, (void **)&j.d_targets,
                           std::max<size_t>(1, j.targets.size()) * sizeof(VgxTarget));
+    if(!rc)
+      rc = list_dev_alloc(l, (void **)&j.d_block_draws, block_draws.size() * sizeof(u32));
     if(rc)
       return rc;
     if(l->pool)
@@ -1314,12 +1330,16 @@ static int list_build(vgpu_list *l)
                          cudaMemcpyHostToDevice, l->pool_stream));
       CK(cudaMemcpyAsync(j.d_targets, j.targets.data(), j.targets.size() * sizeof(VgxTarget),
                          cudaMemcpyHostToDevice, l->pool_stream));
+      CK(cudaMemcpyAsync(j.d_block_draws, block_draws.data(), block_draws.size() * sizeof(u32),
+                         cudaMemcpyHostToDevice, l->pool_stream));
     }
     else
     {
       CK(cudaMemcpy(j.d_draws, j.draws.data(), j.draws.size() * sizeof(VgxDraw),
                     cudaMemcpyHostToDevice));
       CK(cudaMemcpy(j.d_targets, j.targets.data(), j.targets.size() * sizeof(VgxTarget),
+                    cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(j.d_block_draws, block_draws.data(), block_draws.size() * sizeof(u32),
                     cudaMemcpyHostToDevice));
     }
   }
@@ -1525,6 +1545,7 @@ static VgxJob make_job(vgpu_queue *q, vgpu_list *l, Job &j, size_t ji)
   J.records = (u64)(l->d_records + j.rec_off);
   J.counts = (u64)(l->d_counts + j.cnt_off);
   J.first_keys = (u64)(l->d_counts + j.first_off);
+  J.block_draws = (u64)j.d_block_draws;
   J.keys = (u64)q->keys[0];
   J.vals = (u64)q->vals[0];
   J.keys_alt = (u64)q->keys[1];
@@ -1581,7 +1602,7 @@ static int run_setup(vgpu_queue *q, vgpu_list *l, size_t ji)
     return VGPU_OK;
   }
   VgxJob J = make_job(q, l, j, ji);
-  int rc = launch(q, j.var->setup, (j.num_tris + 255) / 256, 256, &J);
+  int rc = launch(q, j.var->setup, (j.num_tris + kSetupBlock - 1) / kSetupBlock, kSetupBlock, &J);
   if(rc)
     return rc;
   u32 *counts = l->d_counts + j.cnt_off;
