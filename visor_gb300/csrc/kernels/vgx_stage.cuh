@@ -36,6 +36,13 @@
 #ifndef VGX_DEFERRED
 #define VGX_DEFERRED 0
 #endif
+/* Immediate-mode jobs whose fragment shader fetches no texels shade each passing
+   fragment inline, in the per-pixel depth loop, instead of queueing it for a
+   32-wide window (the queue pays for itself only with costly shaders). */
+#ifndef VGX_FS_SAMPLES
+#define VGX_FS_SAMPLES 1
+#endif
+#define VGX_INPLACE (!VGX_DEFERRED && VGX_FS_SAMPLES == 0)
 /* Coverage rows of a batch: 1 classifies each triangle's clipped rectangle by its
    corners (fully covered, empty or partly covered) and spreads the partly covered
    rows over the warp; 0 lets each lane walk its own rows, cheaper for jobs of
@@ -481,7 +488,7 @@ struct VgxWarpShared
     };
     u64 rowm[32]; /* per triangle of the batch: its coverage rows, one byte each */
   };
-#if !VGX_DEFERRED
+#if !VGX_DEFERRED && !VGX_INPLACE
   /* fragment queue: passing fragments wait here across batches until 32 can be
      shaded at once; in queue order, so each pixel's fragments stay in primitive order */
   u32 qrec[VGX_QCAP], qown[VGX_QCAP], qst[VGX_QCAP];
@@ -500,7 +507,7 @@ __device__ __forceinline__ VgxPlane vgx_plane_load(const VgxWarpShared &sh, u32 
   return p;
 }
 
-#if !VGX_DEFERRED
+#if !VGX_DEFERRED && !VGX_INPLACE
 /*
  * Shade the first cnt (<= 32) queued fragments, one per lane, then let each
  * pixel's owner lane blend its entries in queue order, and drop them from the
@@ -942,11 +949,35 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
         pass[p] |= 1u << t;
         if(stt & S_DEPTH_WRITE)
           dep[p] = z;
+#if VGX_INPLACE
+        /* perspective correction (rasterizer.cpp:580-588), interpolation, the
+           fragment shader and the blend, in primitive order for this pixel */
+        const u32 *g = (const u32 *)job.records + (u64)pt.b.w * VGX_REC;
+        float nb[4];
+        nb[0] = nn[0] * __uint_as_float(__ldg(g + R_INVW));
+        nb[1] = nn[1] * __uint_as_float(__ldg(g + R_INVW + 1));
+        nb[2] = nn[2] * __uint_as_float(__ldg(g + R_INVW + 2));
+        const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
+        nb[0] = nb[0] * invlen;
+        nb[1] = nb[1] * invlen;
+        nb[2] = nb[2] * invlen;
+        nb[3] = 0.0f;
+        float iv[3 * (VGX_K > 0 ? VGX_K : 1)];
+#pragma unroll
+        for(int q = 0; q < 3 * VGX_K; q++)
+          iv[q] = __uint_as_float(__ldg(g + VGX_REC_HEAD + q));
+        const float4 c = vgx_fs(draws[__ldg(g + R_DRAW)], nb, iv, iv + VGX_K, iv + 2 * VGX_K,
+                                __uint_as_float(__ldg(g + R_LOD)));
+        col[p] = vgx_blend_write(stt, c, col[p]);
+#endif
       }
     }
   }
   shaded_total += __popc(pass[0]) + __popc(pass[1]);
-#if VGX_DEFERRED
+#if VGX_INPLACE
+  (void)qn;
+  (void)last;
+#elif VGX_DEFERRED
   /* deferred: the pixel keeps only its last passing fragment; shaded at the bin's end */
 #pragma unroll
   for(int p = 0; p < 2; p++)

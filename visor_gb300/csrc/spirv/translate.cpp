@@ -465,6 +465,7 @@ struct Gen
   std::map<uint32_t, BlockPtr> bptr;
   std::map<uint32_t, uint32_t> fs_slot_of_var; /* FS input var -> first slot */
   int lod_slot = -1, lod_tex = -1;
+  int samples = 0; /* image sample instructions emitted */
   std::set<uint32_t> emitted_structs;
 
   Gen(const Module &mm) : m(mm) {}
@@ -1090,6 +1091,7 @@ bool Gen::emit_inst(std::ostringstream &o, const Inst &in, const Func &f,
     case OpImageSampleExplicitLod:
     {
       uint32_t img = w[2], coord = w[3];
+      samples++;
       std::string lod = "ctx.lod";
       if(in.op == OpImageSampleExplicitLod && w.size() > 5 && (w[4] & 0x2))
         lod = val(w[5]);
@@ -1612,6 +1614,8 @@ bool translate(const Module *vs, const char *vs_entry, const Module *fs, const c
   src << "#define VGX_K " << k << "\n";
   src << "#define VGX_LOD_SLOT " << gf.lod_slot << "\n";
   src << "#define VGX_LOD_TEX " << (gf.lod_tex < 0 ? 0 : gf.lod_tex) << "\n";
+  /* fragment shaders without texture fetches are cheap enough to run inline */
+  src << "#define VGX_FS_SAMPLES " << gf.samples << "\n";
   src << gv.out.str() << gf.out.str();
 
   /* vertex wrapper */
