@@ -404,84 +404,106 @@ __global__ void k_ranges(const u32 *keys, const u32 *pair_total, u32 capacity, u
   if(n > capacity)
     return;
   const u32 lane = threadIdx.x & 31u;
-  /* the loop bound is uniform per warp: each warp appends its tile heads with one
-     atomic (heads of many small tiles would otherwise queue on one address) */
-  for(u32 i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x)
+  /* Each warp takes 256 consecutive pairs at a time: it counts their tile heads,
+     reserves the heads' work-list slots with a single atomic, then writes the
+     ranges from the same (now cached) keys.  An atomic per 32 pairs queued on
+     one address, and every warp stalled on its round trip. */
+  const u32 nwarps = (gridDim.x * blockDim.x) >> 5;
+  const u32 gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32 lt = (1u << lane) - 1u;
+  for(u64 s0 = (u64)gw * 256u; s0 < n; s0 += (u64)nwarps * 256u)
   {
-    const u32 i = i0 + threadIdx.x;
-    const bool in = i < n;
-    const u32 k = in ? keys[i] : 0u;
-    const bool head = in && (i == 0 || keys[i - 1] != k);
-    const u32 hb = __ballot_sync(0xffffffffu, head);
-    u32 wbase = 0;
-    if(lane == 0 && hb)
-      wbase = atomicAdd(&status[3], (u32)__popc(hb));
-    wbase = __shfl_sync(0xffffffffu, wbase, 0);
-    if(head)
+    const u32 c0 = (u32)s0, c1 = (u32)min((u64)n, s0 + 256u);
+    u32 heads = 0;
+#pragma unroll
+    for(u32 r = 0; r < 8; r++)
     {
-      tstart[k] = i;
-      u32 lo = 0, hi = num_targets - 1;
-      while(lo < hi)
-      {
-        const u32 mid = (lo + hi + 1) >> 1;
-        if((staged ? s_base[mid] : targets[mid].tile_base) <= k)
-          lo = mid;
-        else
-          hi = mid - 1;
-      }
-      work[wbase + __popc(hb & ((1u << lane) - 1u))] = make_uint2(k, lo);
+      const u32 i = c0 + r * 32u + lane;
+      const bool head = i < c1 && (i == 0 || keys[i - 1] != keys[i]);
+      heads += __popc(__ballot_sync(0xffffffffu, head));
     }
-    if(in && (i == n - 1 || keys[i + 1] != k))
-      tend[k] = i + 1;
+    u32 wbase = 0;
+    if(lane == 0 && heads)
+      wbase = atomicAdd(&status[3], heads);
+    wbase = __shfl_sync(0xffffffffu, wbase, 0);
+#pragma unroll 1
+    for(u32 r = 0; r < 8; r++)
+    {
+      const u32 i = c0 + r * 32u + lane;
+      const bool in = i < c1;
+      const u32 k = in ? keys[i] : 0u;
+      const bool head = in && (i == 0 || keys[i - 1] != k);
+      const u32 hb = __ballot_sync(0xffffffffu, head);
+      if(head)
+      {
+        tstart[k] = i;
+        u32 lo = 0, hi = num_targets - 1;
+        while(lo < hi)
+        {
+          const u32 mid = (lo + hi + 1) >> 1;
+          if((staged ? s_base[mid] : targets[mid].tile_base) <= k)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        work[wbase + __popc(hb & lt)] = make_uint2(k, lo);
+      }
+      wbase += __popc(hb);
+      if(in && (i == n - 1 || keys[i + 1] != k))
+        tend[k] = i + 1;
+    }
   }
 }
 
 /* Clear values into the pixels of cleared targets whose bin tile has no
    triangles (tend == 0); tiles with triangles are cleared inside the raster.
-   One grid row per target (strided), four pixels of a row per thread. */
+   One grid row per target (strided); a warp reads the tend words of 32
+   consecutive tiles at once and clears each empty one, four pixels a lane. */
 __global__ void k_clear_empty(const VgxTarget *targets, u32 num_targets, u32 shift, const u32 *tend)
 {
+  const u32 lane = threadIdx.x & 31u;
+  const u32 wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const u32 edge = 1u << shift, quads = (edge * edge) >> 2;
   for(u32 ti = blockIdx.y; ti < num_targets; ti += gridDim.y)
   {
     const VgxTarget T = targets[ti];
     if(!T.init_clear)
       continue;
     const u32 W = (u32)T.width, H = (u32)T.height;
-    const u32 qpr = (W + 3) >> 2;
+    const u32 ntiles = T.tiles_x * T.tiles_y;
     u32 *color = (u32 *)T.color;
     float *depth = (float *)T.depth;
-    /* quad q = y * qpr + xq, advanced by the grid stride without dividing per quad */
-    const u32 stride = gridDim.x * blockDim.x;
-    const u32 sy = stride / qpr, sx = stride - sy * qpr;
-    const u32 q0 = blockIdx.x * blockDim.x + threadIdx.x;
-    u32 y = q0 / qpr, xq = q0 - y * qpr;
-    for(; y < H; y += sy, xq += sx)
+    for(u32 t0 = wid * 32u; t0 < ntiles; t0 += nw * 32u)
     {
-      if(xq >= qpr)
+      const u32 tl = t0 + lane;
+      u32 em = __ballot_sync(0xffffffffu, tl < ntiles && tend[T.tile_base + tl] == 0u);
+      while(em)
       {
-        xq -= qpr;
-        y++;
-        if(y >= H)
-          break;
-      }
-      const u32 x = xq << 2;
-      if(__ldg(tend + T.tile_base + (y >> shift) * T.tiles_x + (x >> shift)))
-        continue;
-      const u64 pix = (u64)y * W + x;
-      if(x + 4 <= W && (pix & 3) == 0)
-      {
-        ((uint4 *)color)[pix >> 2] = make_uint4(T.clear_bgra, T.clear_bgra, T.clear_bgra, T.clear_bgra);
-        if(depth)
-          ((float4 *)depth)[pix >> 2] =
-              make_float4(T.clear_depth, T.clear_depth, T.clear_depth, T.clear_depth);
-      }
-      else
-      {
-        for(u32 i = 0; i < 4 && x + i < W; i++)
+        const u32 tile = t0 + (u32)(__ffs(em) - 1);
+        em &= em - 1;
+        const u32 ty = tile / T.tiles_x, tx = tile - ty * T.tiles_x;
+        for(u32 q = lane; q < quads; q += 32u)
         {
-          color[pix + i] = T.clear_bgra;
-          if(depth)
-            depth[pix + i] = T.clear_depth;
+          const u32 x = (tx << shift) + ((q << 2) & (edge - 1u)), y = (ty << shift) + ((q << 2) >> shift);
+          if(y >= H || x >= W)
+            continue;
+          const u64 pix = (u64)y * W + x;
+          if(x + 4 <= W && (pix & 3) == 0)
+          {
+            ((uint4 *)color)[pix >> 2] = make_uint4(T.clear_bgra, T.clear_bgra, T.clear_bgra, T.clear_bgra);
+            if(depth)
+              ((float4 *)depth)[pix >> 2] =
+                  make_float4(T.clear_depth, T.clear_depth, T.clear_depth, T.clear_depth);
+          }
+          else
+          {
+            for(u32 i = 0; i < 4 && x + i < W; i++)
+            {
+              color[pix + i] = T.clear_bgra;
+              if(depth)
+                depth[pix + i] = T.clear_depth;
+            }
+          }
         }
       }
     }
@@ -1580,12 +1602,12 @@ static int launch(vgpu_queue *q, CUfunction f, unsigned grid, unsigned block, Vg
 /* clears of the empty bin tiles of a job's cleared targets */
 static void launch_clear_empty(cudaStream_t stream, const Job &j, const u32 *tend)
 {
-  u32 max_quads = 1;
+  u32 max_tiles = 1;
   for(const VgxTarget &t : j.targets)
-    max_quads = std::max<u32>(max_quads, (((u32)t.width + 3) >> 2) * (u32)t.height);
+    max_tiles = std::max<u32>(max_tiles, t.tiles_x * t.tiles_y);
   const u32 nt = (u32)j.targets.size();
-  /* about 16 CTAs of 256 threads per SM in total */
-  u32 gx = (max_quads + 255) / 256;
+  /* about 16 CTAs of 256 threads per SM in total; a warp takes 32 tiles at a time */
+  u32 gx = (max_tiles + 255) / 256;
   const u32 want = std::max<u32>(1, (u32)g_sms * 16 / std::max<u32>(nt, 1));
   gx = std::max<u32>(1, std::min(gx, want));
   const u32 gy = std::min<u32>(nt, 65535);
