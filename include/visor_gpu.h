@@ -66,6 +66,10 @@ void vgpu_program_destroy(vgpu_program *p);
 int vgpu_program_check(const char *shader_source, uint32_t tile_shift, char *log, size_t log_size,
                        uint64_t *cubin_bytes);
 uint32_t vgpu_program_record_words(const vgpu_program *p);
+/* Compile now every raster variant a batched job of this program may select (its
+   per-pixel shading modes) for the current bin tiling, so that no later submit
+   waits on NVRTC; the serving engine calls it as requests arrive. */
+int vgpu_program_warm(vgpu_program *p);
 
 /* Command lists: built once per recorded command buffer, replayed per submit. */
 vgpu_list *vgpu_list_create(void);
@@ -184,6 +188,7 @@ typedef struct vgpu_server_stats {
   uint64_t binning_bytes;                       /* slots' binning storage */
   uint32_t max_batch_seen, in_flight;
   uint64_t tris, shaded;                        /* over completed batches */
+  uint64_t peak_device_bytes;                   /* peak of admitted requests' bytes + binning storage */
 } vgpu_server_stats;
 
 int vgpu_server_create(const vgpu_server_config *cfg, vgpu_server **out);

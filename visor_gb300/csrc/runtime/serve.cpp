@@ -224,6 +224,7 @@ void start_raster(vgpu_server *S, Slot &sl)
   std::lock_guard<std::mutex> g(S->mu);
   S->binning = b;
   S->stats.binning_bytes = b;
+  S->stats.peak_device_bytes = std::max(S->stats.peak_device_bytes, S->reserved + b);
 }
 
 /* Stage 2 finished: the batch's results are in host memory. */
@@ -259,10 +260,20 @@ void launch_batch(vgpu_server *S, Slot &sl)
     std::lock_guard<std::mutex> g(S->mu);
     uint64_t tris = 0;
     const uint64_t room = S->cfg.budget_bytes > S->binning ? S->cfg.budget_bytes - S->binning : 0;
+    /* the slot's tile arrays grow to the batch's bin tiles before it runs: that growth
+       is charged against the budget as requests join the batch */
+    vgpu_tuning tun;
+    vgpu_get_tuning(&tun);
+    const uint32_t shift = std::min<uint32_t>(std::max<uint32_t>(tun.bin_shift, 3), 6);
+    const uint64_t have_tiles = vgpu_queue_tile_capacity(sl.q);
+    uint64_t batch_tiles = 0, grow = 0;
     while(!S->pending.empty() && sl.reqs.size() < S->cfg.max_batch)
     {
       Req *r = S->pending.front();
-      if(r->need > room)
+      const uint64_t rt = (uint64_t)((r->r.width + (1u << shift) - 1) >> shift) *
+                          ((r->r.height + (1u << shift) - 1) >> shift);
+      const uint64_t g = batch_tiles + rt > have_tiles ? (batch_tiles + rt - have_tiles) * 16 : 0;
+      if(r->need + (rt > have_tiles ? (rt - have_tiles) * 16 : 0) > room)
       {
         S->pending.pop_front();
         std::vector<Req *> one{r};
@@ -272,7 +283,7 @@ void launch_batch(vgpu_server *S, Slot &sl)
         complete_locked(S, one, VGPU_ERROR_OUT_OF_DEVICE_MEMORY, vgpu_now_ns(), false);
         continue;
       }
-      if(S->reserved + r->need > room)
+      if(S->reserved + r->need + g > room)
         break; /* wait for memory: admission stays in arrival order */
       if(!sl.reqs.empty() && tris + r->tris > S->cfg.max_batch_tris)
         break;
@@ -280,12 +291,26 @@ void launch_batch(vgpu_server *S, Slot &sl)
       S->reserved += r->need;
       S->in_flight++;
       S->stats.peak_reserved_bytes = std::max(S->stats.peak_reserved_bytes, S->reserved);
+      S->stats.peak_device_bytes = std::max(S->stats.peak_device_bytes, S->reserved + S->binning + g);
       r->admit_ns = vgpu_now_ns();
       tris += r->tris;
+      batch_tiles += rt;
+      grow = g;
       sl.reqs.push_back(r);
     }
     if(sl.reqs.empty())
       return;
+    if(grow)
+    {
+      /* grow the tile arrays now, inside the budget the admissions above kept */
+      const int trc = vgpu_queue_reserve_binning(sl.q, 0, (uint32_t)std::min<uint64_t>(batch_tiles, 0xffffffffull));
+      uint64_t b = 0;
+      for(Slot &o : S->slots)
+        b += vgpu_queue_binning_bytes(o.q);
+      S->binning = b;
+      S->stats.binning_bytes = b;
+      (void)trc;
+    }
     S->stats.max_batch_seen = std::max<uint32_t>(S->stats.max_batch_seen, (uint32_t)sl.reqs.size());
   }
   int rc = VGPU_OK;
@@ -456,6 +481,7 @@ extern "C" int vgpu_server_create(const vgpu_server_config *cfg, vgpu_server **o
     S->binning += vgpu_queue_binning_bytes(sl.q);
   }
   S->stats.binning_bytes = S->binning;
+  S->stats.peak_device_bytes = S->binning;
   if(S->binning >= S->cfg.budget_bytes)
   {
     fprintf(stderr, "visor_gb300: serving budget %llu bytes does not cover the slots' binning storage (%llu)\n",
@@ -472,6 +498,11 @@ extern "C" int vgpu_server_submit(vgpu_server *S, const vgpu_request *r, uint64_
 {
   if(!r->program || !r->width || !r->height || r->width > kMaxTargetEdge || r->height > kMaxTargetEdge)
     return VGPU_ERROR_INITIALIZATION_FAILED;
+  /* a batch may select any shading mode of the program: compile them before the
+     request waits behind a batch that would otherwise compile one */
+  const int wrc = vgpu_program_warm(r->program);
+  if(wrc)
+    return wrc;
   Req *q = new Req();
   q->r = *r;
   if(!q->r.arrival_ns)
@@ -480,8 +511,10 @@ extern "C" int vgpu_server_submit(vgpu_server *S, const vgpu_request *r, uint64_
   const uint64_t px = (uint64_t)r->width * r->height;
   const uint64_t rec = vgpu_program_record_words(r->program);
   /* target, triangle records, tile counts and their scan levels, descriptors */
+  /* counts, their scan levels, single-tile bin keys and the per-block draw table */
   q->need = align256(px * 4) + align256(px * 4) + align256(q->tris * rec * 4) +
-            align256((q->tris + 1) * 4 + (q->tris / 1024 + 64) * 4) + 4096;
+            align256((q->tris + 1) * 4 + (q->tris / 1024 + 64) * 4 + q->tris * 4) +
+            align256((q->tris / 256 + 1) * 4) + 4096;
   {
     std::lock_guard<std::mutex> g(S->mu);
     q->ticket = S->next_ticket++;

@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -730,6 +731,7 @@ struct vgpu_program
   u32 k = 0, rec_words = 0;
   std::map<u32, VgpuVariant *> variants; /* key: tile_shift << 8 | warps */
   std::mutex mu;
+  std::atomic<u32> warm_gen{0}; /* tuning generation whose variants are all compiled */
 };
 
 static int compile_cubin(const std::string &src, std::vector<char> &cubin, char *log, size_t log_size)
@@ -931,6 +933,21 @@ extern "C" void vgpu_program_destroy(vgpu_program *p)
 }
 
 extern "C" uint32_t vgpu_program_record_words(const vgpu_program *p) { return p->rec_words; }
+
+extern "C" int vgpu_program_warm(vgpu_program *p)
+{
+  if(!p)
+    return VGPU_ERROR_INITIALIZATION_FAILED;
+  const u32 gen = g_tuning_gen;
+  if(p->warm_gen.load() == gen)
+    return VGPU_OK;
+  int rc = VGPU_OK;
+  for(u32 mode = 0; mode <= 2; mode++)
+    if(!get_variant(p, g_tuning.bin_shift, g_tuning.raster_warps, mode, &rc))
+      return rc;
+  p->warm_gen.store(gen);
+  return VGPU_OK;
+}
 
 /* ------------------------------------------------------------------------ */
 /* command lists                                                             */
@@ -2550,16 +2567,28 @@ extern "C" int vgpu_list_phase_b(vgpu_queue *q, vgpu_list *l)
 
 extern "C" uint64_t vgpu_queue_binning_bytes(const vgpu_queue *q)
 {
-  return (u64)q->pair_capacity * 16 + q->hist_words * 4 + (u64)q->tile_capacity * 12 +
+  /* pairs: keys and values, twice (sort ping-pong); tiles: start, end, work entry */
+  return (u64)q->pair_capacity * 16 + q->hist_words * 4 + (u64)q->tile_capacity * 16 +
          q->scratch_words * 4;
 }
 
 extern "C" int vgpu_queue_reserve_binning(vgpu_queue *q, uint64_t pairs, uint32_t tiles)
 {
-  int rc = ensure_pairs(q, (u32)std::min<uint64_t>(pairs, 0xffffffffull));
+  const u32 p = (u32)std::min<uint64_t>(pairs, 0xffffffffull);
+  int rc = ensure_pairs(q, p);
   if(!rc)
     rc = ensure_tiles(q, tiles);
+  if(!rc)
+  {
+    /* the scan scratch a sort of that many pairs uses */
+    std::vector<u64> lv;
+    u64 need = 0;
+    hist_levels(std::max<u32>(p, 1), lv, need);
+    rc = ensure_scratch(q, need + 4);
+  }
   return rc;
 }
+
+extern "C" uint32_t vgpu_queue_tile_capacity(const vgpu_queue *q) { return q->tile_capacity; }
 
 extern "C" int vgpu_device_ordinal(void) { return g_device; }

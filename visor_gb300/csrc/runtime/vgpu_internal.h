@@ -35,6 +35,8 @@ int vgpu_queue_reserve_binning(vgpu_queue *q, uint64_t pairs, uint32_t tiles);
 int vgpu_device_ordinal(void);
 /* Bytes of binning storage the queue holds (pairs, sort, tile ranges, scratch). */
 uint64_t vgpu_queue_binning_bytes(const vgpu_queue *q);
+/* Bin tiles the queue's tile arrays hold (16 bytes each). */
+uint32_t vgpu_queue_tile_capacity(const vgpu_queue *q);
 
 #ifdef __cplusplus
 }
