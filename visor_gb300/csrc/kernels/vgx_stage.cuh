@@ -90,11 +90,6 @@ __device__ __forceinline__ u32 vgx_find_draw(const VgxDraw *draws, u32 n, u32 tr
   return lo;
 }
 
-__device__ __forceinline__ u32 vgx_count_tiles(const int *r)
-{
-  return vgx_visit_tiles(r, VGX_TILE_SHIFT, [](u32, int, int) {});
-}
-
 __device__ __forceinline__ void vgx_warp_add_u64(u64 *dst, u64 v)
 {
   unsigned long long s = v;
@@ -381,17 +376,6 @@ __device__ __forceinline__ void vgx_bary(const u32 *r, int x, int y, int &b0, in
   b0 = ((int)r[R_AREA2] - (ux + uy)) * bm;
   b1 = ux * bm;
   b2 = uy * bm;
-}
-
-__device__ __forceinline__ bool vgx_covers(const u32 *r, int x, int y)
-{
-  u32 mn = r[R_MIN], mx = r[R_MAX];
-  if(x < (int)(mn & 0xffffu) || x >= (int)(mx & 0xffffu) || y < (int)(mn >> 16) ||
-     y >= (int)(mx >> 16))
-    return false;
-  int b0, b1, b2;
-  vgx_bary(r, x, y, b0, b1, b2);
-  return (b0 | b1 | b2) >= 0;
 }
 
 __device__ __forceinline__ float vgx_pixdepth(const u32 *r, int b0, int b1, int b2, float *n)
