@@ -463,15 +463,7 @@ struct VgxWarpShared
     float4 col[32];
     u16 item[256]; /* coverage rows to test: triangle << 11 | column mask << 3 | row */
   };
-  union
-  {
-    struct
-    {
-      u32 frag[32]; /* deferred window: triangle record */
-      u32 fown[32]; /* deferred window: owner lane | pixel-half << 5 */
-    };
-    u64 rowm[32]; /* per triangle of the batch: its coverage rows, one byte each */
-  };
+  u64 rowm[32]; /* per triangle of the batch: its coverage rows, one byte each */
 #if !VGX_DEFERRED && !VGX_INPLACE
   /* fragment queue: passing fragments wait here across batches until 32 can be
      shaded at once; in queue order, so each pixel's fragments stay in primitive order */
@@ -824,7 +816,7 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     }
     else
     {
-      __syncwarp(); /* the arrays alias the shading window, read by other lanes before */
+      __syncwarp(); /* the item array aliases the shading window, read by other lanes before */
       sh.rowm[lane] = direct;
       for(u32 j = 0; j < prows; j++)
         sh.item[incl - prows + j] = (u16)(((u32)lane << 11) | (pitem + j));
@@ -1042,118 +1034,79 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
 #if VGX_DEFERRED
 /*
  * Deferred shading of one 8x8 sub-tile of an all-opaque job: every pixel with a
- * passing fragment shades it once, in windows of 32 fragments (one per lane),
- * and the owner lane writes the colour bytes.  Barycentrics are evaluated from
- * the triangle record exactly as rasterizer.cpp:303-309 does.
+ * passing fragment shades it once, each lane its own two pixels in turn (no
+ * gathering into windows: the pixels of most sub-tiles are covered), and writes
+ * the colour bytes.  Barycentrics are evaluated from the triangle record exactly
+ * as rasterizer.cpp:303-309 does, then perspective correction (:580-588).
  */
-__device__ __forceinline__ void vgx_shade_deferred(const VgxJob &job, VgxWarpShared &sh, int lane,
-                                                   int x0, int y0, const u32 *vis, u32 *col)
+__device__ __forceinline__ void vgx_shade_deferred(const VgxJob &job, int lane, int x0, int y0,
+                                                   const u32 *vis, u32 *col)
 {
   const VgxDraw *draws = (const VgxDraw *)job.draws;
-  const u32 mine = (vis[0] != 0xffffffffu ? 1u : 0u) + (vis[1] != 0xffffffffu ? 1u : 0u);
-  u32 incl = mine;
-#pragma unroll
-  for(int o = 1; o < 32; o <<= 1)
+#pragma unroll 1
+  for(int p = 0; p < 2; p++)
   {
-    u32 v = __shfl_up_sync(0xffffffffu, incl, o);
-    if(lane >= o)
-      incl += v;
-  }
-  const u32 total = __shfl_sync(0xffffffffu, incl, 31);
-  const u32 excl = incl - mine;
-  for(u32 chunk = 0; chunk < total; chunk += 32)
-  {
-    u32 k = excl;
+    if(vis[p] == 0xffffffffu)
+      continue;
+    const u32 rec = vis[p];
+    const int px = x0 + (lane & 7), py = y0 + (lane >> 3) + 4 * p;
+    const u32 *g = (const u32 *)job.records + (u64)rec * VGX_REC;
+    u32 h[VGX_REC_HEAD];
 #pragma unroll
-    for(int p = 0; p < 2; p++)
-      if(vis[p] != 0xffffffffu)
-      {
-        if(k >= chunk && k < chunk + 32)
-        {
-          sh.frag[k - chunk] = vis[p];
-          sh.fown[k - chunk] = (u32)lane | ((u32)p << 5);
-        }
-        k++;
-      }
-    __syncwarp();
-    if(chunk + lane < total)
+    for(int q = 0; q < VGX_REC_HEAD; q += 4)
     {
-      const u32 rec = sh.frag[lane], own = sh.fown[lane];
-      const int px = x0 + (int)(own & 7), py = y0 + (int)((own >> 3) & 3) + 4 * (int)(own >> 5);
-      const u32 *g = (const u32 *)job.records + (u64)rec * VGX_REC;
-      /* the record header as 16-byte loads (records are 16-byte aligned) */
-      u32 h[VGX_REC_HEAD];
-#pragma unroll
-      for(int q = 0; q < VGX_REC_HEAD; q += 4)
-      {
-        const uint4 v = __ldg((const uint4 *)(g + q));
-        h[q] = v.x;
-        h[q + 1] = v.y;
-        h[q + 2] = v.z;
-        h[q + 3] = v.w;
-      }
-      int b0, b1, b2;
-      vgx_bary(h, px, py, b0, b1, b2);
-      const float ia = __uint_as_float(h[R_INVAREA]);
-      float nb[4];
-      nb[0] = (float)b0 * ia;
-      nb[1] = (float)b1 * ia;
-      nb[2] = (float)b2 * ia;
-      /* perspective correction, rasterizer.cpp:580-588 */
-      nb[0] = nb[0] * __uint_as_float(h[R_INVW]);
-      nb[1] = nb[1] * __uint_as_float(h[R_INVW + 1]);
-      nb[2] = nb[2] * __uint_as_float(h[R_INVW + 2]);
-      const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
-      nb[0] = nb[0] * invlen;
-      nb[1] = nb[1] * invlen;
-      nb[2] = nb[2] * invlen;
-      nb[3] = 0.0f;
-      const VgxDraw &D = draws[h[R_DRAW]];
-      float iv[3][VGX_K > 0 ? VGX_K : 1];
+      const uint4 v = __ldg((const uint4 *)(g + q));
+      h[q] = v.x;
+      h[q + 1] = v.y;
+      h[q + 2] = v.z;
+      h[q + 3] = v.w;
+    }
+    int b0, b1, b2;
+    vgx_bary(h, px, py, b0, b1, b2);
+    const float ia = __uint_as_float(h[R_INVAREA]);
+    float nb[4];
+    nb[0] = (float)b0 * ia;
+    nb[1] = (float)b1 * ia;
+    nb[2] = (float)b2 * ia;
+    nb[0] = nb[0] * __uint_as_float(h[R_INVW]);
+    nb[1] = nb[1] * __uint_as_float(h[R_INVW + 1]);
+    nb[2] = nb[2] * __uint_as_float(h[R_INVW + 2]);
+    const float invlen = 1.0f / (nb[0] + nb[1] + nb[2]);
+    nb[0] = nb[0] * invlen;
+    nb[1] = nb[1] * invlen;
+    nb[2] = nb[2] * invlen;
+    nb[3] = 0.0f;
+    const VgxDraw &D = draws[h[R_DRAW]];
+    float iv[3][VGX_K > 0 ? VGX_K : 1];
 #if VGX_DEFERRED == 2
-      /* the vertex shader again for the triangle's three vertices (deterministic, so
-         the interpolants equal the ones setup computed) */
-      u32 vidx[3];
-      (void)vgx_tri_indices(D, rec - D.tri_base, vidx);
+    u32 vidx[3];
+    (void)vgx_tri_indices(D, rec - D.tri_base, vidx);
+#pragma unroll
+    for(int v = 0; v < 3; v++)
+    {
+      float4 pos;
+      vgx_vs(D, vidx[v], pos, iv[v]);
+    }
+#else
+    {
+      float w[(3 * VGX_K + 3) & ~3];
+#pragma unroll
+      for(int q = 0; q < 3 * VGX_K; q += 4)
+      {
+        const uint4 v = __ldg((const uint4 *)(g + VGX_REC_HEAD + q));
+        w[q] = __uint_as_float(v.x);
+        w[q + 1] = __uint_as_float(v.y);
+        w[q + 2] = __uint_as_float(v.z);
+        w[q + 3] = __uint_as_float(v.w);
+      }
 #pragma unroll
       for(int v = 0; v < 3; v++)
-      {
-        float4 pos;
-        vgx_vs(D, vidx[v], pos, iv[v]);
-      }
-#else
-      {
-        /* the interpolants as 16-byte loads (a record is padded to a multiple of 4 words) */
-        float w[(3 * VGX_K + 3) & ~3];
 #pragma unroll
-        for(int q = 0; q < 3 * VGX_K; q += 4)
-        {
-          const uint4 v = __ldg((const uint4 *)(g + VGX_REC_HEAD + q));
-          w[q] = __uint_as_float(v.x);
-          w[q + 1] = __uint_as_float(v.y);
-          w[q + 2] = __uint_as_float(v.z);
-          w[q + 3] = __uint_as_float(v.w);
-        }
-#pragma unroll
-        for(int v = 0; v < 3; v++)
-#pragma unroll
-          for(int q = 0; q < VGX_K; q++)
-            iv[v][q] = w[v * VGX_K + q];
-      }
-#endif
-      sh.col[lane] = vgx_fs(D, nb, iv[0], iv[1], iv[2], __uint_as_float(h[R_LOD]));
+        for(int q = 0; q < VGX_K; q++)
+          iv[v][q] = w[v * VGX_K + q];
     }
-    __syncwarp();
-    k = excl;
-#pragma unroll
-    for(int p = 0; p < 2; p++)
-      if(vis[p] != 0xffffffffu)
-      {
-        if(k >= chunk && k < chunk + 32)
-          col[p] = vgx_blend_write(0u, sh.col[k - chunk], col[p]);
-        k++;
-      }
-    __syncwarp();
+#endif
+    col[p] = vgx_blend_write(0u, vgx_fs(D, nb, iv[0], iv[1], iv[2], __uint_as_float(h[R_LOD])), col[p]);
   }
 }
 #endif
@@ -1336,7 +1289,7 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
 #pragma unroll
     for(int j = 0; j < VGX_SUBS_PER_WARP; j++)
       if(valid[j])
-        vgx_shade_deferred(job, sh, lane, sx[j], sy[j], vis[j], col[j]);
+        vgx_shade_deferred(job, lane, sx[j], sy[j], vis[j], col[j]);
 #endif
 
 #pragma unroll
