@@ -280,25 +280,25 @@ extern "C" __global__ void __launch_bounds__(256, 4) vgx_setup(VgxJob job)
   const bool big = has_rec && vgx_bbox_tiles(r, VGX_TILE_SHIFT) > VGX_COOP_TILES;
   if(has_rec && !big)
   {
-    int ftx = 0, fty = 0;
+    u32 k0 = 0, k1 = 0;
     ntiles = vgx_visit_tiles(r, VGX_TILE_SHIFT, [&](u32 i, int tx, int ty) {
+      const u32 key = tbase + (u32)ty * tcols + (u32)tx;
       if(i == 0)
-      {
-        ftx = tx;
-        fty = ty;
-      }
+        k0 = key;
+      else if(i == 1)
+        k1 = key;
     });
-    /* a triangle in one bin tile is emitted from this key without its record */
-    if(ntiles == 1 && job.first_keys)
-      ((u32 *)job.first_keys)[tri] = tbase + (u32)fty * tcols + (u32)ftx;
+    /* a triangle in one or two bin tiles is emitted from these keys without its record */
+    if(ntiles - 1u < 2u && job.first_keys)
+      *(uint2 *)((u32 *)job.first_keys + 2 * (u64)tri) = make_uint2(k0, k1);
   }
-  /* a big bbox can still touch a single tile (a triangle mostly off-screen): the
-     first tile's key is left for every triangle the warp walks */
+  /* a big bbox can still touch one or two tiles (a triangle mostly off-screen): the
+     first tiles' keys are left for every triangle the warp walks */
   const u32 pay[4] = {tri, tbase, tcols, job.first_keys ? 1u : 0u};
   const u32 coop = vgx_coop_visit_tiles(r, big, VGX_TILE_SHIFT, (int)(threadIdx.x & 31), pay,
                                         [&](const u32 *p, u32 i, int tx, int ty) {
-                                          if(i == 0 && p[3])
-                                            ((u32 *)job.first_keys)[p[0]] = p[1] + (u32)ty * p[2] + (u32)tx;
+                                          if(i < 2 && p[3])
+                                            ((u32 *)job.first_keys)[2 * (u64)p[0] + i] = p[1] + (u32)ty * p[2] + (u32)tx;
                                         });
   if(big)
     ntiles = coop;

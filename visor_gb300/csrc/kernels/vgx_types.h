@@ -136,7 +136,7 @@ typedef struct VgxJob {
   u64 status;                         /* u32*: [0] flags, [1] pair total, [2] work queue, [3] work count */
   u64 counters;                       /* u64*: tris_out, tested, covered, shaded, depth-tested */
   u64 scratch;                        /* u32* scan/sort scratch */
-  u64 first_keys;                     /* u32* per triangle: its bin tile, for triangles in one tile */
+  u64 first_keys;                     /* uint2* per triangle: its first two bin tiles (one- or two-tile triangles) */
   u64 block_draws;                    /* u32* per setup block of 256 triangles: the draw of its first */
   u32 num_draws, num_tris;
   u32 num_targets, num_tiles;

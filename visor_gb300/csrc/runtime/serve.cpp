@@ -511,9 +511,9 @@ extern "C" int vgpu_server_submit(vgpu_server *S, const vgpu_request *r, uint64_
   const uint64_t px = (uint64_t)r->width * r->height;
   const uint64_t rec = vgpu_program_record_words(r->program);
   /* target, triangle records, tile counts and their scan levels, descriptors */
-  /* counts, their scan levels, single-tile bin keys and the per-block draw table */
+  /* counts, their scan levels, the one- and two-tile bin keys and the per-block draw table */
   q->need = align256(px * 4) + align256(px * 4) + align256(q->tris * rec * 4) +
-            align256((q->tris + 1) * 4 + (q->tris / 1024 + 64) * 4 + q->tris * 4) +
+            align256((q->tris + 1) * 4 + (q->tris / 1024 + 64) * 4 + q->tris * 8 + 8) +
             align256((q->tris / 256 + 1) * 4) + 4096;
   {
     std::lock_guard<std::mutex> g(S->mu);

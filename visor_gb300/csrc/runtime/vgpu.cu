@@ -239,11 +239,17 @@ __global__ void k_emit(VgxJob job, u32 rec_words, const u32 *offsets)
     off = offsets[tri];
     const u32 n = offsets[tri + 1] - off;
     active = n != 0;
-    if(n == 1 && job.first_keys)
+    if(n - 1u < 2u && job.first_keys)
     {
-      /* one bin tile: setup left its key */
-      keys[off] = ((const u32 *)job.first_keys)[tri];
+      /* one or two bin tiles: setup left their keys */
+      const uint2 k = *((const uint2 *)job.first_keys + tri);
+      keys[off] = k.x;
       vals[off] = tri;
+      if(n == 2)
+      {
+        keys[off + 1] = k.y;
+        vals[off + 1] = tri;
+      }
       active = false;
     }
   }
@@ -1342,8 +1348,9 @@ static int list_build(vgpu_list *l)
       j.scan_levels.push_back(cnt_words);
       cnt_words += n + 1;
     }
+    cnt_words = (cnt_words + 1) & ~1ull; /* the key pairs are read as 8-byte words */
     j.first_off = cnt_words;
-    cnt_words += j.num_tris;
+    cnt_words += 2 * (u64)j.num_tris;
     /* the draw of each setup block's first triangle (draws are in tri_base order) */
     std::vector<u32> &block_draws = j.block_draws;
     block_draws.assign(std::max<u32>(1, (j.num_tris + kSetupBlock - 1) / kSetupBlock), 0u);
