@@ -125,13 +125,15 @@ void *vgpu_queue_stream(vgpu_queue *q);
 int vgpu_queue_flush_l2(vgpu_queue *q);
 
 /* Tuning knobs read at list build time (autotuner, see tune.py).  A list is built
-   again on its next vgpu_submit after bin_shift or raster_warps change. */
+   again on its next vgpu_submit after bin_shift, raster_warps or setup_counts change. */
 typedef struct vgpu_tuning {
   uint32_t raster_blocks_per_sm; /* persistent raster CTAs per SM (0: 32 warps' worth) */
   uint32_t use_graphs;           /* replay batched lists as CUDA graphs */
   uint32_t time_raster;          /* record CUDA events around raster launches (vgpu_stats.raster_ms) */
   uint32_t bin_shift;            /* bin tile edge 2^bin_shift pixels (3..6: 8x8 .. 64x64) */
   uint32_t raster_warps;         /* warps per bin tile (each owns 8x8 sub-tiles) */
+  uint32_t setup_counts;         /* covered pixels counted in setup, depth rejection before coverage:
+                                    0 never, 1 always, 2 for jobs averaging 256+ triangles per bin */
 } vgpu_tuning;
 void vgpu_set_tuning(const vgpu_tuning *t);
 void vgpu_get_tuning(vgpu_tuning *t);

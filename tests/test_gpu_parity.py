@@ -73,16 +73,19 @@ VARIANT_SCENES = ["blend_overlap", "depth_lequal", "offscreen", "guard_band", "g
                   "cfg1_sphere", "cfg2_small_blend", "cfg3_small_trilinear", "cfg4_small"]
 
 
-@pytest.mark.parametrize("variant", [(4, 1), (4, 4), (5, 8), (5, 16), (6, 16)])
+@pytest.mark.parametrize("variant", [(4, 1, 0), (4, 4, 0), (5, 8, 0), (5, 16, 0), (6, 16, 0), (3, 1, 1), (4, 4, 1),
+                                     (5, 16, 1)])
 @pytest.mark.parametrize("name", VARIANT_SCENES)
 def test_bin_variants_match_oracle(device, oracle, name, variant):
-    """Every bin tile / warps-per-bin configuration the autotuner may pick renders identically."""
-    vg.set_tuning(bin_shift=variant[0], raster_warps=variant[1])
+    """Every bin tile / warps-per-bin configuration the autotuner may pick renders identically,
+    with covered pixels counted by the raster or (variant[2]) in setup with depth rejection
+    before coverage rows."""
+    vg.set_tuning(bin_shift=variant[0], raster_warps=variant[1], setup_counts=variant[2])
     try:
         h = scenes_edge.build(vg.lib(), name)
         gc, gd, gk = vg.render(h, vg.MODE_BATCHED, device)
     finally:
-        vg.set_tuning(bin_shift=3, raster_warps=1)
+        vg.set_tuning(bin_shift=3, raster_warps=1, setup_counts=2)
     ho = scenes_edge.build(oracle.lib, name)
     oc, od, ok = oracle.render(ho)
     _compare(gc, gd, oc, od)

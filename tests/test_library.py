@@ -52,10 +52,12 @@ def test_translated_shaders_compile_for_sm103a(shader):
     assert vg.nvrtc_check(src) > 10000
 
 
-@pytest.mark.parametrize("shift,warps,deferred,blocks", [(4, 4, 0, 0), (4, 4, 2, 0), (3, 1, 1, 1), (5, 8, 0, 1)])
-def test_raster_variants_compile_for_sm103a(shift, warps, deferred, blocks):
+@pytest.mark.parametrize("shift,warps,deferred,blocks,counts",
+                         [(4, 4, 0, 0, 0), (4, 4, 2, 0, 0), (3, 1, 1, 1, 0), (5, 8, 0, 1, 0), (4, 4, 0, 0, 1),
+                          (3, 1, 1, 0, 1)])
+def test_raster_variants_compile_for_sm103a(shift, warps, deferred, blocks, counts):
     src = vg.translate(vg.spirv(vs.SHADER_LAMBERT_TEX, 0), vg.spirv(vs.SHADER_LAMBERT_TEX, 4))
-    assert vg.nvrtc_check(src, shift, warps, deferred, blocks) > 10000
+    assert vg.nvrtc_check(src, shift, warps, deferred, blocks, counts) > 10000
 
 
 def test_translator_rejects_garbage():

@@ -44,7 +44,8 @@ class VgpuStats(C.Structure):
 
 class VgpuTuning(C.Structure):
     _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("use_graphs", C.c_uint32),
-                ("time_raster", C.c_uint32), ("bin_shift", C.c_uint32), ("raster_warps", C.c_uint32)]
+                ("time_raster", C.c_uint32), ("bin_shift", C.c_uint32), ("raster_warps", C.c_uint32),
+                ("setup_counts", C.c_uint32)]
 
 
 def lib():
@@ -126,15 +127,15 @@ def translate(vs_words, fs_words):
     return out.value.decode()
 
 
-def nvrtc_check(source, tile_shift=3, warps=1, deferred=0, blocks=0):
+def nvrtc_check(source, tile_shift=3, warps=1, deferred=0, blocks=0, counts=0):
     """NVRTC-compile translated source with the stage kernels for sm_103a; returns cubin bytes.
 
-    deferred (0..2) and blocks (block-compressed textures) select the raster
-    variants the runtime builds for such jobs."""
+    deferred (0..2), blocks (block-compressed textures) and counts (covered pixels
+    counted in setup) select the raster variants the runtime builds for such jobs."""
     L = lib()
     log = C.create_string_buffer(65536)
     nbytes = C.c_uint64(0)
-    key = tile_shift | (warps << 8) | (deferred << 16) | ((1 if blocks else 0) << 18)
+    key = tile_shift | (warps << 8) | (deferred << 16) | ((1 if blocks else 0) << 18) | ((1 if counts else 0) << 19)
     rc = L.vgpu_program_check(source.encode(), key, log, 65536, C.byref(nbytes))
     if rc != 0:
         raise RuntimeError("NVRTC failed:\n" + log.value.decode())
@@ -146,7 +147,7 @@ def set_mode(mode):
 
 
 def set_tuning(raster_blocks_per_sm=None, use_graphs=None, time_raster=None, bin_shift=None,
-               raster_warps=None):
+               raster_warps=None, setup_counts=None):
     """Runtime knobs read when a command buffer is lowered (autotuned by visor_gb300.tune)."""
     L = lib()
     t = VgpuTuning()
@@ -161,6 +162,8 @@ def set_tuning(raster_blocks_per_sm=None, use_graphs=None, time_raster=None, bin
         t.use_graphs = use_graphs
     if time_raster is not None:
         t.time_raster = time_raster
+    if setup_counts is not None:
+        t.setup_counts = setup_counts
     L.vgpu_set_tuning(C.byref(t))
 
 

@@ -50,6 +50,18 @@
 #ifndef VGX_ROW_SPREAD
 #define VGX_ROW_SPREAD (VGX_DEFERRED != 2)
 #endif
+/* 1: setup counts the covered pixels of triangles inside the target with exact edge
+   functions, so the raster builds no coverage for those that depth rejects; others
+   carry S_RASTER_COUNT and the raster counts them from their masks.  Chosen by the
+   host for jobs with many triangles per bin (deep overdraw, where depth rejects
+   most of them); needs the spread row phase. */
+#ifndef VGX_SETUP_COUNTS
+#define VGX_SETUP_COUNTS 0
+#endif
+#if !VGX_ROW_SPREAD
+#undef VGX_SETUP_COUNTS
+#define VGX_SETUP_COUNTS 0
+#endif
 #if VGX_DEFERRED == 2
 #define VGX_REC VGX_REC_HEAD
 #else
@@ -67,7 +79,8 @@
    triangles by bbox before batching them */
 #define VGX_SUB_FILTER (VGX_SUBS_PER_WARP == 1 && VGX_SUBS > 1)
 
-/* state word */
+/* state word (bit 19, S_EXACT, is defined with the record words) */
+#define S_RASTER_COUNT (1u << 20) /* covered pixels counted by the raster, not by setup */
 #define S_DEPTH_OP(s) ((s)&7u)
 #define S_DEPTH_WRITE 8u
 #define S_BLEND 16u
@@ -75,6 +88,80 @@
 #define S_DST(s) (((s) >> 10) & 31u)
 #define S_DEPTH_TEST 32768u
 #define S_BLEND_OP(s) (((s) >> 16) & 7u)
+
+/* Greatest common divisor (binary method; gcd(a, 0) = a). */
+__device__ __forceinline__ u32 vgx_gcd(u32 a, u32 b)
+{
+  if(a == 0)
+    return b;
+  if(b == 0)
+    return a;
+  const int sh = __ffs(a | b) - 1;
+  a >>= __ffs(a) - 1;
+  do
+  {
+    b >>= __ffs(b) - 1;
+    if(a > b)
+    {
+      const u32 t = a;
+      a = b;
+      b = t;
+    }
+    b -= a;
+  } while(b);
+  return a << sh;
+}
+
+/*
+ * Covered pixels of a triangle whose vertices lie inside the target and whose edge
+ * functions are exact (S_EXACT): the per-pixel test (rasterizer.cpp:543-549) accepts
+ * the lattice points of the closed triangle, and by Pick's theorem there are
+ * (|area2| + boundary points) / 2 + 1 of them; the pixel loop (:538-541) skips the
+ * bbox's last column and last row, which meet the triangle in a vertex or along an
+ * axis-aligned edge, and their shared corner belongs to both only when it is a vertex.
+ */
+__device__ __forceinline__ u32 vgx_count_closed(const int *wx, const int *wy, int area2)
+{
+  const int mx = max(max(wx[0], wx[1]), wx[2]), my = max(max(wy[0], wy[1]), wy[2]);
+  u32 boundary = 0;
+#pragma unroll
+  for(int e = 0; e < 3; e++)
+  {
+    const int f = (e + 1) % 3;
+    boundary += vgx_gcd((u32)abs(wx[f] - wx[e]), (u32)abs(wy[f] - wy[e]));
+  }
+  const u32 closed = ((u32)abs(area2) + boundary) / 2u + 1u;
+  u32 col = 0, row = 0, corner = 0;
+  int ex = -1, ey = -1;
+#pragma unroll
+  for(int v = 0; v < 3; v++)
+  {
+    if(wx[v] == mx)
+    {
+      col++;
+      ex = ex < 0 ? v : ex;
+    }
+    if(wy[v] == my)
+    {
+      row++;
+      ey = ey < 0 ? v : ey;
+    }
+    corner |= (wx[v] == mx && wy[v] == my) ? 1u : 0u;
+  }
+  /* two vertices on the last column (row): the edge between them lies on it */
+  u32 on_col = 1, on_row = 1;
+  if(col == 2)
+  {
+    const int o = wx[(ex + 1) % 3] == mx ? (ex + 1) % 3 : (ex + 2) % 3;
+    on_col = (u32)abs(wy[o] - wy[ex]) + 1u;
+  }
+  if(row == 2)
+  {
+    const int o = wy[(ey + 1) % 3] == my ? (ey + 1) % 3 : (ey + 2) % 3;
+    on_row = (u32)abs(wx[o] - wx[ey]) + 1u;
+  }
+  return closed - on_col - on_row + corner;
+}
 
 __device__ __forceinline__ u32 vgx_find_draw(const VgxDraw *draws, u32 n, u32 tri)
 {
@@ -161,6 +248,7 @@ extern "C" __global__ void __launch_bounds__(256, 4) vgx_setup(VgxJob job)
   int r[VGX_REC_HEAD] = {0}; /* the triangle's record header when has_rec */
   bool has_rec = false;
   u32 ntiles = 0, tbase = 0, tcols = 0;
+  u32 setup_covered = 0; /* covered pixels counted here (VGX_SETUP_COUNTS) */
   if(live)
   {
     u32 di = s_draw;
@@ -260,6 +348,16 @@ extern "C" __global__ void __launch_bounds__(256, 4) vgx_setup(VgxJob job)
                    ((D.blend_op & 7u) << 16);
           if(vgx_span_safe(r))
             st |= S_EXACT;
+#if VGX_SETUP_COUNTS
+          {
+            const int vminx = min(min(wx[0], wx[1]), wx[2]), vminy = min(min(wy[0], wy[1]), wy[2]);
+            const int vmaxx = max(max(wx[0], wx[1]), wx[2]), vmaxy = max(max(wy[0], wy[1]), wy[2]);
+            if((st & S_EXACT) && vminx >= 0 && vminy >= 0 && vmaxx <= T.width - 1 && vmaxy <= T.height - 1)
+              setup_covered = vgx_count_closed(wx, wy, area2);
+            else
+              st |= S_RASTER_COUNT;
+          }
+#endif
           r[R_STATE] = (int)st;
           u32 *rec = (u32 *)job.records + (u64)tri * VGX_REC;
 #pragma unroll
@@ -309,6 +407,9 @@ extern "C" __global__ void __launch_bounds__(256, 4) vgx_setup(VgxJob job)
   if((threadIdx.x & 31) == 0 && kb)
     atomicAdd((unsigned long long *)&cnt[0], (unsigned long long)__popc(kb));
   vgx_warp_add_u64(&cnt[1], tested);
+#if VGX_SETUP_COUNTS
+  vgx_warp_add_u64(&cnt[2], setup_covered);
+#endif
 }
 
 /* Depth compare of ProcessTriangles (rasterizer.cpp:562-576). */
@@ -568,6 +669,35 @@ __device__ __forceinline__ void vgx_queue_shade(const VgxJob &job, VgxWarpShared
 }
 #endif
 
+/* Conservative depth rejection of a whole triangle (coverage `has`) against the
+   sub-tile's depth range [tmin, tmax], valid while no triangle of the batch can move
+   a stored depth the other way (any_raise / any_lower). */
+__device__ __forceinline__ bool vgx_hiz_reject(bool has, u32 st, bool finite, float dlo, float dhi,
+                                               float tmin, float tmax, bool any_raise, bool any_lower)
+{
+  const u32 op = S_DEPTH_OP(st);
+  if(!has || !(st & S_DEPTH_TEST))
+    return false;
+  if(op == 0u)
+    return true;
+  if(finite && !any_raise && ((op == 1u && dlo >= tmax) || (op == 3u && dlo > tmax)))
+    return true;
+  if(finite && !any_lower && ((op == 4u && dhi <= tmin) || (op == 6u && dhi < tmin)))
+    return true;
+  return finite && !any_raise && !any_lower && op == 2u && (dlo > tmax || dhi < tmin);
+}
+
+/* may a triangle with coverage `has` and state `st` raise / lower a stored depth? */
+__device__ __forceinline__ bool vgx_may_raise(bool has, u32 st)
+{
+  return has && (st & S_DEPTH_WRITE) && !((st & S_DEPTH_TEST) && S_DEPTH_OP(st) <= 3u);
+}
+__device__ __forceinline__ bool vgx_may_lower(bool has, u32 st)
+{
+  const u32 op = S_DEPTH_OP(st);
+  return has && (st & S_DEPTH_WRITE) && !((st & S_DEPTH_TEST) && (op == 0u || op == 2u || op == 4u || op == 6u));
+}
+
 /*
  * One warp, one 8x8 sub-tile at (x0, y0), one batch of n <= 32 triangles whose
  * record headers lane t holds in r[] (triangle t).  Lane L owns pixels
@@ -582,6 +712,22 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
 {
   const VgxDraw *draws = (const VgxDraw *)job.draws;
   const int ldx = lane & 7, ldy = lane >> 3;
+
+  /* the sub-tile's stored depth range (hierarchical depth rejection) */
+  float tmax = __int_as_float(0xff800000), tmin = __int_as_float(0x7f800000);
+#pragma unroll
+  for(int p = 0; p < 2; p++)
+    if(in[p])
+    {
+      tmax = fmaxf(tmax, dep[p]);
+      tmin = fminf(tmin, dep[p]);
+    }
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1)
+  {
+    tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+    tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
+  }
 
   /* lane t: its triangle's planes at the sub-tile origin, coverage mask, depth bounds */
   u32 mlo = 0, mhi = 0, st = 0;
@@ -765,6 +911,22 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     }
   }
 #endif
+#if VGX_SETUP_COUNTS
+  {
+    /* Triangles whose pixels setup counted need no coverage where depth rejects them
+       whole: decided here, before their rows are tested (a triangle's rectangle that
+       the corners did not show empty stands in for its coverage). */
+    const bool rect = prows != 0 || direct != 0;
+    const bool early_raise = __any_sync(0xffffffffu, vgx_may_raise(rect, st));
+    const bool early_lower = __any_sync(0xffffffffu, vgx_may_lower(rect, st));
+    if(!(st & S_RASTER_COUNT) &&
+       vgx_hiz_reject(rect, st, finite, dlo, dhi, tmin, tmax, early_raise, early_lower))
+    {
+      prows = 0;
+      direct = 0;
+    }
+  }
+#endif
   /* Rows of partly covered rectangles (and of triangles without exact corner
      arithmetic) are tested pixel by pixel: each row is walked from dx = 7 down to
      0, shifting each pixel's inside bit (all three edge values non-negative) in at
@@ -851,44 +1013,14 @@ __device__ __forceinline__ void vgx_subtile_batch(const VgxJob &job, VgxWarpShar
     }
   }
 #endif
-  covered_total += __popc(mlo) + __popc(mhi);
+  if(!VGX_SETUP_COUNTS || (st & S_RASTER_COUNT))
+    covered_total += __popc(mlo) + __popc(mhi);
 
   /* conservative depth rejection of whole triangles against the sub-tile's depth range */
-  float tmax = __int_as_float(0xff800000), tmin = __int_as_float(0x7f800000);
-#pragma unroll
-  for(int p = 0; p < 2; p++)
-    if(in[p])
-    {
-      tmax = fmaxf(tmax, dep[p]);
-      tmin = fminf(tmin, dep[p]);
-    }
-#pragma unroll
-  for(int o = 16; o > 0; o >>= 1)
-  {
-    tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
-    tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
-  }
   const bool has = (mlo | mhi) != 0;
-  const u32 op = S_DEPTH_OP(st);
-  const bool writes = has && (st & S_DEPTH_WRITE);
-  const bool tested = (st & S_DEPTH_TEST) != 0;
-  /* can any triangle of this batch raise (lower) a stored depth? */
-  const bool raises = writes && !(tested && op <= 3u);
-  const bool lowers = writes && !(tested && (op == 0u || op == 2u || op == 4u || op == 6u));
-  const bool any_raise = __any_sync(0xffffffffu, raises);
-  const bool any_lower = __any_sync(0xffffffffu, lowers);
-  bool skip = false;
-  if(has && tested)
-  {
-    if(op == 0u)
-      skip = true;
-    else if(finite && !any_raise && ((op == 1u && dlo >= tmax) || (op == 3u && dlo > tmax)))
-      skip = true;
-    else if(finite && !any_lower && ((op == 4u && dhi <= tmin) || (op == 6u && dhi < tmin)))
-      skip = true;
-    else if(finite && !any_raise && !any_lower && op == 2u && (dlo > tmax || dhi < tmin))
-      skip = true;
-  }
+  const bool any_raise = __any_sync(0xffffffffu, vgx_may_raise(has, st));
+  const bool any_lower = __any_sync(0xffffffffu, vgx_may_lower(has, st));
+  const bool skip = vgx_hiz_reject(has, st, finite, dlo, dhi, tmin, tmax, any_raise, any_lower);
   const u32 live = __ballot_sync(0xffffffffu, has && !skip);
   __syncwarp();
 

@@ -117,7 +117,7 @@ std::mutex g_mu;
 bool g_init = false;
 int g_sms = 148;
 int g_device = 0;
-vgpu_tuning g_tuning = {0, 1, 0, 3, 1};
+vgpu_tuning g_tuning = {0, 1, 0, 3, 1, 2};
 u32 g_tuning_gen = 1; /* bumped when a knob that shapes lists (bin tile, warps) changes */
 
 /* ------------------------------------------------------------------------ */
@@ -727,6 +727,8 @@ struct VgpuVariant
   CUfunction setup = nullptr, raster = nullptr;
   u32 tile_shift = 3, warps = 1;
   u32 deferred = 0; /* shading mode: 0 immediate, 1/2 each pixel's last fragment once (all-opaque jobs) */
+  u32 blocks = 0;   /* block-compressed texel decoding compiled in */
+  u32 counts = 0;   /* setup counts covered pixels; depth rejection before coverage rows */
   u32 rec_words = 0; /* triangle record size: the header only when deferred */
 };
 
@@ -780,9 +782,11 @@ static int compile_cubin(const std::string &src, std::vector<char> &cubin, char 
 }
 
 static std::string full_source(const char *shader_source, uint32_t tile_shift, uint32_t warps = 1,
-                               uint32_t deferred = 0, uint32_t blocks = 0)
+                               uint32_t deferred = 0, uint32_t blocks = 0, uint32_t counts = 0)
 {
   std::string src;
+  /* covered pixels counted in setup and depth rejection before coverage rows */
+  src += "#define VGX_SETUP_COUNTS " + std::to_string(counts ? 1 : 0) + "\n";
   /* block-compressed texel decoding only where a job binds such a texture */
   src += "#define VGX_TEX_BLOCKS " + std::to_string(blocks ? 1 : 0) + "\n";
   src += "#define VGX_TILE_SHIFT " + std::to_string(tile_shift) + "\n";
@@ -800,10 +804,10 @@ extern "C" int vgpu_program_check(const char *shader_source, uint32_t tile_shift
                                   size_t log_size, uint64_t *cubin_bytes)
 {
   std::vector<char> cubin;
-  /* tile_shift carries the warps per bin in bits 8..15, the shading mode in bits 16..17 and
-     block-compressed texture support in bit 18 */
+  /* tile_shift carries the warps per bin in bits 8..15, the shading mode in bits 16..17,
+     block-compressed texture support in bit 18 and setup counting in bit 19 */
   int rc = compile_cubin(full_source(shader_source, tile_shift & 0xff, std::max(1u, (tile_shift >> 8) & 0xff),
-                                     (tile_shift >> 16) & 3, (tile_shift >> 18) & 1),
+                                     (tile_shift >> 16) & 3, (tile_shift >> 18) & 1, (tile_shift >> 19) & 1),
                          cubin, log, log_size);
   if(cubin_bytes)
     *cubin_bytes = cubin.size();
@@ -861,22 +865,23 @@ static int load_cubin(const std::string &src, std::vector<char> &cubin, char *lo
 /* The variant of a program for a bin tile edge of 2^tile_shift pixels and
    `warps` warps per bin; compiled with NVRTC on first use. */
 static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, u32 deferred,
-                                int *rc_out, u32 blocks = 0)
+                                int *rc_out, u32 blocks = 0, u32 counts = 0)
 {
   tile_shift = std::min<u32>(std::max<u32>(tile_shift, 3), 6);
   const u32 subs = 1u << (2 * (tile_shift - 3));
   warps = std::max<u32>(1, std::min<u32>(warps, std::min<u32>(subs, 16)));
   deferred = std::min<u32>(deferred, 2);
   blocks = blocks ? 1 : 0;
-  const u32 key = blocks << 18 | deferred << 16 | tile_shift << 8 | warps;
+  counts = counts && deferred != 2 ? 1 : 0; /* the tiny-triangle variant has no spread rows */
+  const u32 key = counts << 19 | blocks << 18 | deferred << 16 | tile_shift << 8 | warps;
   std::lock_guard<std::mutex> lk(p->mu);
   auto it = p->variants.find(key);
   if(it != p->variants.end())
     return it->second;
   std::vector<char> cubin;
   char log[4096] = {0};
-  int rc = load_cubin(full_source(p->source.c_str(), tile_shift, warps, deferred, blocks), cubin, log,
-                      sizeof(log));
+  int rc = load_cubin(full_source(p->source.c_str(), tile_shift, warps, deferred, blocks, counts), cubin,
+                      log, sizeof(log));
   if(rc)
   {
     *rc_out = rc;
@@ -886,6 +891,8 @@ static VgpuVariant *get_variant(vgpu_program *p, u32 tile_shift, u32 warps, u32 
   v->tile_shift = tile_shift;
   v->warps = warps;
   v->deferred = deferred;
+  v->blocks = blocks;
+  v->counts = counts;
   v->rec_words = deferred == 2 ? 20u : p->rec_words;
   if(cudaSetDevice(g_device) != cudaSuccess || g_cu.moduleLoadData(&v->mod, cubin.data()) != CUDA_SUCCESS ||
      g_cu.moduleGetFunction(&v->setup, v->mod, "vgx_setup") != CUDA_SUCCESS ||
@@ -1327,10 +1334,11 @@ static int list_build(vgpu_list *l)
       for(int k = 0; k < VGX_MAX_TEX; k++)
         if(d.tex[k].base && d.tex[k].format != VGX_TEX_RGBA8)
           blocks = 1;
-    if(mode || blocks)
+    const u32 counts = g_tuning.setup_counts == 1 ? 1u : 0u;
+    if(mode || blocks || counts)
     {
       int vrc = VGPU_OK;
-      VgpuVariant *dv = get_variant(j.prog, j.var->tile_shift, j.var->warps, mode, &vrc, blocks);
+      VgpuVariant *dv = get_variant(j.prog, j.var->tile_shift, j.var->warps, mode, &vrc, blocks, counts);
       if(!dv)
         return vrc;
       j.var = dv;
@@ -1929,6 +1937,24 @@ static int record_raster_fixed(vgpu_queue *q, vgpu_list *l, size_t ji, u32 cap)
 static int capture_graph(vgpu_queue *q, vgpu_list *l)
 {
   graph_forget(l);
+  /* With the pair totals of the first submit known: jobs averaging many triangles
+     per bin (deep overdraw, most of it rejected by depth) count covered pixels in
+     setup and skip coverage rows of rejected triangles. */
+  if(g_tuning.setup_counts == 2)
+    for(size_t i = 0; i < l->jobs.size(); i++)
+    {
+      Job &j = l->jobs[i];
+      const u32 want = j.num_tris && l->h_totals[i] >= 256ull * std::max<u32>(j.num_tiles, 1u) ? 1u : 0u;
+      if(want != j.var->counts && !(want && j.var->deferred == 2))
+      {
+        int vrc = VGPU_OK;
+        VgpuVariant *v = get_variant(j.prog, j.var->tile_shift, j.var->warps, j.var->deferred, &vrc,
+                                     j.var->blocks, want);
+        if(!v)
+          return vrc;
+        j.var = v;
+      }
+    }
   std::vector<u32> cap(l->jobs.size(), 0);
   u32 maxcap = 0, maxtiles = 0, rasters = 0;
   u64 scratch = 0, pairs = 0;
@@ -2227,7 +2253,8 @@ extern "C" void vgpu_queue_reset_stats(vgpu_queue *q)
 
 extern "C" void vgpu_set_tuning(const vgpu_tuning *t)
 {
-  if(t->bin_shift != g_tuning.bin_shift || t->raster_warps != g_tuning.raster_warps)
+  if(t->bin_shift != g_tuning.bin_shift || t->raster_warps != g_tuning.raster_warps ||
+     t->setup_counts != g_tuning.setup_counts)
     g_tuning_gen++;
   g_tuning = *t;
 }
