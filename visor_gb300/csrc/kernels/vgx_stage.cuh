@@ -1346,15 +1346,56 @@ extern "C" __global__ void __launch_bounds__(VGX_RASTER_WARPS * 32) vgx_raster(V
         while(cq < 32 && base < end)
         {
           const u32 n = min(32u, end - base);
+#if VGX_SETUP_COUNTS
+          /* Where stored depths can only fall (job.monotone), a triangle whose pixels
+             setup counted and whose nearest vertex already fails the test against the
+             sub-tile's farthest stored depth is dropped here too: the depths can only
+             get nearer before its turn comes. */
+          float tfar = __int_as_float(0xff800000);
+          if(job.monotone)
+          {
+#pragma unroll
+            for(int p = 0; p < 2; p++)
+              if(in[0][p])
+                tfar = fmaxf(tfar, dep[0][p]);
+#pragma unroll
+            for(int o = 16; o > 0; o >>= 1)
+              tfar = fmaxf(tfar, __shfl_xor_sync(0xffffffffu, tfar, o));
+          }
+#endif
           bool keep = false;
           u32 ri = 0;
           if((u32)lane < n)
           {
             ri = vals[base + lane];
-            const uint2 bb = __ldg((const uint2 *)((const u32 *)job.records + (u64)ri * VGX_REC + R_MIN));
+            static_assert(R_MIN == 8 && R_MAX == 9 && R_STATE == 11 && R_DEPTH == 13, "record words read as vectors");
+            const u32 *g = (const u32 *)job.records + (u64)ri * VGX_REC;
+#if VGX_SETUP_COUNTS
+            const uint4 bb = __ldg((const uint4 *)(g + 8));
+#else
+            const uint2 bb = __ldg((const uint2 *)(g + 8));
+#endif
             const int minx = (int)(bb.x & 0xffffu), miny = (int)(bb.x >> 16);
             const int maxx = (int)(bb.y & 0xffffu), maxy = (int)(bb.y >> 16);
             keep = minx < sx[0] + 8 && maxx > sx[0] && miny < sy[0] + 8 && maxy > sy[0];
+#if VGX_SETUP_COUNTS
+            const u32 st = bb.w;
+            if(keep && job.monotone && (st & S_DEPTH_TEST) && !(st & S_RASTER_COUNT))
+            {
+              const uint4 dz = __ldg((const uint4 *)(g + 12));
+              const float d0 = __uint_as_float(dz.y), d1 = __uint_as_float(dz.z), d2 = __uint_as_float(dz.w);
+              const u32 op = S_DEPTH_OP(st);
+              if(op == 0u)
+                keep = false;
+              else if(isfinite(d0) && isfinite(d1) && isfinite(d2))
+              {
+                const float mag = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
+                const float dlo = fminf(d0, fminf(d1, d2)) - (mag * 2.0e-6f + 1.0e-30f);
+                if((op == 1u && dlo >= tfar) || ((op == 2u || op == 3u) && dlo > tfar))
+                  keep = false;
+              }
+            }
+#endif
           }
           const u32 kb = __ballot_sync(0xffffffffu, keep);
           if(keep)

@@ -1005,6 +1005,7 @@ struct Job
   std::vector<VgxTarget> targets;
   std::vector<u64> target_keys; /* colour address identifies a target */
   u32 num_tris = 0, num_tiles = 0, key_bits = 1, all_tiles = 0, all_opaque = 1;
+  u32 monotone = 1; /* no draw can raise a stored depth */
   u64 first_off = 0; /* word offset of the per-triangle first bin keys in the count arena */
   /* device */
   VgxDraw *d_draws = nullptr;
@@ -1307,6 +1308,10 @@ static int list_build(vgpu_list *l)
     d.target = tidx;
     if(d.blend_enable)
       open->all_opaque = 0;
+    /* a depth write untested (ALWAYS) or under GREATER / NOT_EQUAL / GEQUAL can raise
+       a stored depth */
+    if(open->targets[tidx].depth && d.depth_write && (d.depth_op & 7u) > 3u)
+      open->monotone = 0;
     d.tri_base = open->num_tris;
     open->num_tris += ntris;
     open->draws.push_back(d);
@@ -1619,6 +1624,7 @@ static VgxJob make_job(vgpu_queue *q, vgpu_list *l, Job &j, size_t ji)
   J.key_bits = j.key_bits;
   J.all_tiles = j.all_tiles;
   J.all_opaque = j.all_opaque;
+  J.monotone = j.monotone;
   (void)ji;
   return J;
 }
