@@ -67,8 +67,9 @@ def test_gpu_matches_oracle(device, oracle, name, mode):
     assert gk == ref["counters"]
 
 
-VARIANT_SCENES = ["blend_overlap", "depth_lequal", "offscreen", "guard_band", "guard_band_blend", "corner_sliver",
-                  "strip",
+VARIANT_SCENES = ["blend_overlap", "depth_lequal", "depth_less", "depth_equal", "depth_never", "depth_greater",
+                  "depth_gequal", "depth_not_equal", "depth_always", "degenerate", "shared_edges", "offscreen",
+                  "guard_band", "guard_band_blend", "corner_sliver", "strip",
                   "texture_wrap", "load_pass",
                   "cfg1_sphere", "cfg2_small_blend", "cfg3_small_trilinear", "cfg4_small"]
 
