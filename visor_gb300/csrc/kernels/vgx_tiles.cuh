@@ -113,7 +113,7 @@ __device__ __forceinline__ u32 vgx_bbox_tiles(const int *r, u32 shift)
 }
 
 /* triangles spanning more bin tiles than this are walked by the whole warp */
-#define VGX_COOP_TILES 8u
+#define VGX_COOP_TILES 16u
 
 /*
  * Warp-cooperative form of vgx_visit_tiles for the lanes with `big` set (all 32
