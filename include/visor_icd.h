@@ -66,6 +66,16 @@ VkResult visor_gb300_swapchain_read(VkSwapchainKHR swapchain, uint32_t index, vo
 void visor_gb300_set_mode(int mode);
 int visor_gb300_get_mode(void);
 
+/* Draw parameters for command buffers lowered after this call.  0 (default): the
+   reference's behaviour, which ignores vertexOffset, instanceCount and firstInstance
+   and fetches every vertex attribute per vertex (cmd_exec.cpp:129-142,
+   rasterizer.cpp:100-119).  1: their Vulkan meaning, with per-instance input rate
+   and gl_InstanceIndex; an instanced draw is lowered as draws of up to 2^30
+   triangles of whole instances.  The environment variable
+   VISOR_GB300_DRAW_PARAMETERS=vulkan sets the initial value. */
+void visor_gb300_set_draw_parameters(int vulkan);
+int visor_gb300_get_draw_parameters(void);
+
 /* Queue statistics (rasterizer counters, launches, device time of the last submit). */
 int visor_gb300_queue_stats(VkQueue queue, vgpu_stats *out);
 void visor_gb300_queue_reset_stats(VkQueue queue);

@@ -34,6 +34,7 @@ enum {
   VSC_SHADER_COLOR = 2,             /* clip-space pos + RGBA8 colour; colour pass-through */
   VSC_SHADER_LAMBERT_TEX_ALPHA = 3, /* as LAMBERT_TEX plus a per-vertex alpha written to .w */
   VSC_SHADER_CUBE = 4,              /* LAMBERT_TEX vertices; samplerCube read at the interpolated normal */
+  VSC_SHADER_COLOR_INSTANCED = 5,   /* COLOR with clip x moved by float(gl_InstanceIndex) * 0.25 */
 };
 
 /* Vertex layouts implied by each shader (bytes per vertex). */
@@ -70,6 +71,12 @@ typedef struct vsc_pipeline {
   uint32_t src_factor;   /* VSC_BLEND_* */
   uint32_t dst_factor;   /* VSC_BLEND_* */
   uint32_t filter;       /* VSC_FILTER_* */
+  /* 0, or 1 + the location of an attribute that comes from vertex binding 1
+     (tightly packed, VK_VERTEX_INPUT_RATE_INSTANCE) instead of binding 0.  The
+     reference steps no attribute per instance, so the oracle renders no such
+     pipeline; the tests compare it, under Vulkan draw parameters, with an
+     equivalent scene of per-vertex attributes. */
+  uint32_t instance_attr;
 } vsc_pipeline;
 
 /* texture formats (texture_sampling.cpp:93-118 decodes the block formats) */
@@ -100,6 +107,13 @@ typedef struct vsc_draw {
   uint32_t push_size; /* bytes of push constants set before the draw */
   uint64_t vb_offset; /* byte offset bound with vkCmdBindVertexBuffers */
   uint8_t push[128];
+  /* draw parameters the reference ignores (cmd_exec.cpp:129-142); they take
+     effect only where Vulkan draw parameters are switched on */
+  int32_t vertex_offset;   /* vkCmdDrawIndexed vertexOffset */
+  uint32_t instances;      /* instanceCount; 0 records 1, VSC_NONE records 0 */
+  uint32_t first_instance; /* firstInstance */
+  uint32_t reserved;
+  uint64_t inst_vb_offset; /* byte offset bound to binding 1 (pipelines with instance_attr) */
 } vsc_draw;
 
 typedef struct vsc_pass {

@@ -446,6 +446,15 @@ static void vs_color(const draw_ctx *c, uint32_t index, vcache *out)
   out->interps[0] = fetch_attr(c, 1, index);
 }
 
+/* COLOR with x += float(gl_InstanceIndex) * 0.25; the reference stores 0 into
+   gl_InstanceIndex (spirv_compile.cpp:1946-1949) */
+static void vs_color_instanced(const draw_ctx *c, uint32_t index, vcache *out)
+{
+  vs_color(c, index, out);
+  const int instance = 0;
+  out->position.v[0] = out->position.v[0] + (float)instance * 0.25f;
+}
+
 /*
  * FS: n = normalize(in0); l = max(dot(n, light.xyz), 0); t = texture(tex, in1);
  * colour = t * l  [or vec4(t.xyz * l, in2) with alpha].
@@ -522,6 +531,7 @@ static void run_vs(const draw_ctx *c, uint32_t index, vcache *out)
     case VSC_SHADER_CUBE: vs_lambert(c, index, out, 0); break;
     case VSC_SHADER_LAMBERT_TEX_ALPHA: vs_lambert(c, index, out, 1); break;
     case VSC_SHADER_COLOR: vs_color(c, index, out); break;
+    case VSC_SHADER_COLOR_INSTANCED: vs_color_instanced(c, index, out); break;
     default: break;
   }
 }
@@ -532,7 +542,8 @@ static f4 run_fs(const draw_ctx *c, const tri_ctx *t, f4 bary)
   {
     case VSC_SHADER_LAMBERT_TEX: return fs_lambert(c, t, bary, 0);
     case VSC_SHADER_LAMBERT_TEX_ALPHA: return fs_lambert(c, t, bary, 1);
-    case VSC_SHADER_COLOR: return fs_color(t, bary);
+    case VSC_SHADER_COLOR:
+    case VSC_SHADER_COLOR_INSTANCED: return fs_color(t, bary);
     case VSC_SHADER_CUBE: return fs_cube(c, t, bary);
     default:
     {
@@ -858,9 +869,21 @@ static void draw_triangles(draw_ctx *c)
 static int render_band(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
                        float **depths, vor_counters *counters, int y0, int y1, int count_prims);
 
+/* The reference steps no attribute per instance (rasterizer.cpp:100-232): a scene
+   whose pipeline asks for one is not a scene it renders. */
+static int scene_supported(const vsc_scene *s)
+{
+  for(uint32_t di = 0; di < s->num_draws; di++)
+    if(s->pipelines[s->draws[di].pipeline].instance_attr)
+      return 0;
+  return 1;
+}
+
 int vor_render_passes(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
                       float **depths, vor_counters *counters)
 {
+  if(!scene_supported(s))
+    return -2;
   return render_band(s, first, count, colors, depths, counters, 0, INT_MAX, 1);
 }
 
@@ -944,6 +967,8 @@ static void *band_main(void *arg)
 int vor_render_threads(const vsc_scene *s, uint32_t first, uint32_t count, uint8_t **colors,
                        float **depths, vor_counters *counters, uint32_t threads)
 {
+  if(!scene_supported(s))
+    return -2;
   uint32_t maxh = 1;
   for(uint32_t t = 0; t < s->num_targets; t++)
     maxh = s->targets[t].height > maxh ? s->targets[t].height : maxh;

@@ -45,7 +45,8 @@ def test_loader_negotiation_and_proc_addr():
     assert not L.vk_icdGetInstanceProcAddr(None, b"vkNotAFunction")
 
 
-@pytest.mark.parametrize("shader", [vs.SHADER_LAMBERT_TEX, vs.SHADER_COLOR, vs.SHADER_LAMBERT_TEX_ALPHA])
+@pytest.mark.parametrize("shader", [vs.SHADER_LAMBERT_TEX, vs.SHADER_COLOR, vs.SHADER_LAMBERT_TEX_ALPHA,
+                                    vs.SHADER_COLOR_INSTANCED])
 def test_translated_shaders_compile_for_sm103a(shader):
     src = vg.translate(vg.spirv(shader, 0), vg.spirv(shader, 4))
     assert "vgx_vs" in src and "vgx_fs" in src

@@ -85,6 +85,8 @@ def lib():
     L.vspv_emit.restype = C.c_size_t
     L.visor_gb300_set_mode.argtypes = [C.c_int]
     L.visor_gb300_get_mode.restype = C.c_int
+    L.visor_gb300_set_draw_parameters.argtypes = [C.c_int]
+    L.visor_gb300_get_draw_parameters.restype = C.c_int
     L.visor_gb300_queue_stats.argtypes = [VP, C.POINTER(VgpuStats)]
     L.visor_gb300_queue_stats.restype = C.c_int
     L.visor_gb300_queue_reset_stats.argtypes = [VP]
@@ -144,6 +146,17 @@ def nvrtc_check(source, tile_shift=3, warps=1, deferred=0, blocks=0, counts=0):
 
 def set_mode(mode):
     lib().visor_gb300_set_mode(mode)
+
+
+def set_draw_parameters(vulkan):
+    """True: vertexOffset, instanceCount, firstInstance and per-instance vertex input take
+    their Vulkan meaning in command buffers lowered from now on.  False (the default, or
+    VISOR_GB300_DRAW_PARAMETERS unset): the reference's behaviour, which ignores all four."""
+    lib().visor_gb300_set_draw_parameters(1 if vulkan else 0)
+
+
+def draw_parameters():
+    return bool(lib().visor_gb300_get_draw_parameters())
 
 
 def set_tuning(raster_blocks_per_sm=None, use_graphs=None, time_raster=None, bin_shift=None,

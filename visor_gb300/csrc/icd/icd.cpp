@@ -166,6 +166,7 @@ struct VkPipeline_T
     uint32_t format = 0, binding = 0, offset = 0;
   } attrs[VGX_MAX_ATTRS];
   uint32_t strides[VGX_MAX_VB] = {0, 0, 0, 0};
+  uint32_t instance_rate = 0; /* bit b: binding b has VK_VERTEX_INPUT_RATE_INSTANCE */
   uint32_t topology = 3, cull = 0, front = 0, depth_op = VK_COMPARE_OP_ALWAYS, depth_write = 0;
   uint32_t blend = 0, src = 1, dst = 0, op = 0;
   vgpu_program *prog = nullptr;
@@ -221,6 +222,25 @@ int default_mode()
   }
   return g_mode;
 }
+
+/* Draw parameters: 0 keeps the reference's behaviour, which ignores vertexOffset,
+   instanceCount and firstInstance and fetches every attribute per vertex
+   (cmd_exec.cpp:129-142, rasterizer.cpp:100-119); 1 gives them their Vulkan
+   meaning.  Read when a command buffer is lowered (its first submit). */
+int g_draw_params = -1;
+
+int draw_parameters()
+{
+  if(g_draw_params < 0)
+  {
+    const char *e = getenv("VISOR_GB300_DRAW_PARAMETERS");
+    g_draw_params = (e && strcmp(e, "vulkan") == 0) ? 1 : 0;
+  }
+  return g_draw_params;
+}
+
+/* triangles of one lowered draw; an instanced draw beyond it is split by instances */
+constexpr uint64_t kDrawTriCap = 1ull << 30;
 
 template <typename T>
 T *mk()
@@ -839,8 +859,13 @@ VISOR_EXPORT VkResult vkCreateGraphicsPipelines(VkDevice dev, VkPipelineCache, u
     const VkPipelineVertexInputStateCreateInfo *vi = ci.pVertexInputState;
     uint32_t strides[16] = {0};
     for(uint32_t b = 0; vi && b < vi->vertexBindingDescriptionCount; b++)
-      if(vi->pVertexBindingDescriptions[b].binding < 16)
-        strides[vi->pVertexBindingDescriptions[b].binding] = vi->pVertexBindingDescriptions[b].stride;
+    {
+      const VkVertexInputBindingDescription &bd = vi->pVertexBindingDescriptions[b];
+      if(bd.binding < 16)
+        strides[bd.binding] = bd.stride;
+      if(bd.binding < VGX_MAX_VB && bd.inputRate == VK_VERTEX_INPUT_RATE_INSTANCE)
+        p->instance_rate |= 1u << bd.binding;
+    }
     for(uint32_t a = 0; vi && a < vi->vertexAttributeDescriptionCount; a++)
     {
       const VkVertexInputAttributeDescription &d = vi->pVertexAttributeDescriptions[a];
@@ -1510,8 +1535,30 @@ void lower(VkCommandBuffer c)
         d.first = b.first;
         fill_draw_state(d, p, s.sets, b.count, [&](VkDeviceMemory_T *m) { note_read(use, m); });
         memcpy(d.push, s.push, 128);
-        if(d.num_tris)
+        d.instances = 1;
+        d.instance_tris = d.num_tris;
+        if(!draw_parameters())
+        {
+          if(d.num_tris)
+            vgpu_list_draw(l, p->prog, &d, &s.target);
+          break;
+        }
+        /* Vulkan draw parameters: instances run in order, each the whole primitive
+           list; sub-draws of whole instances keep a draw's triangle ids in range */
+        d.vertex_offset = k == Pkt::DrawIndexed ? b.vertex_offset : 0;
+        d.instance_rate = p->instance_rate;
+        if(!d.instance_tris)
+          break;
+        const uint32_t per = (uint32_t)std::max<uint64_t>(1, kDrawTriCap / d.instance_tris);
+        for(uint32_t i0 = 0; i0 < b.instances;)
+        {
+          const uint32_t n = std::min(per, b.instances - i0);
+          d.first_instance = b.first_instance + i0;
+          d.instances = n;
+          d.num_tris = (uint32_t)((uint64_t)n * d.instance_tris);
           vgpu_list_draw(l, p->prog, &d, &s.target);
+          i0 += n;
+        }
         break;
       }
       case Pkt::CopyBuf2Img:
@@ -2043,6 +2090,8 @@ VISOR_EXPORT VkResult visor_gb300_server_submit(vgpu_server *server, const visor
   d.first = r->first;
   VkDescriptorSet_T *sets[8] = {r->set};
   fill_draw_state(d, p, sets, r->count, [](VkDeviceMemory_T *) {});
+  d.instances = 1;
+  d.instance_tris = d.num_tris;
   memcpy(d.push, r->push, r->push_size);
   VkClearColorValue cc;
   memcpy(cc.float32, r->clear_color, sizeof(cc.float32));
@@ -2058,6 +2107,11 @@ VISOR_EXPORT VkResult visor_gb300_server_submit(vgpu_server *server, const visor
 }
 
 VISOR_EXPORT void visor_gb300_set_mode(int mode) { g_mode = mode; }
+/* 1: vertexOffset, instanceCount, firstInstance and per-instance vertex input rate
+   take their Vulkan meaning in command buffers lowered from now on; 0: the
+   reference's behaviour (all ignored) */
+VISOR_EXPORT void visor_gb300_set_draw_parameters(int vulkan) { g_draw_params = vulkan ? 1 : 0; }
+VISOR_EXPORT int visor_gb300_get_draw_parameters(void) { return draw_parameters(); }
 VISOR_EXPORT int visor_gb300_get_mode(void) { return default_mode(); }
 
 VISOR_EXPORT int visor_gb300_queue_stats(VkQueue q, vgpu_stats *out) { return vgpu_queue_stats(q->q, out); }

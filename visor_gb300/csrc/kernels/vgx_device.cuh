@@ -22,9 +22,10 @@ __device__ __forceinline__ void vgx_init_unorm8()
  * Vertex attribute fetch with the semantics of GetVertexAttributeData
  * (spirv_compile.cpp:572-627): default (0,0,0,1); 32-bit formats copy as many
  * lanes as they have; RGBA8 UNORM decodes byte/255.  Reads outside the bound
- * buffer return the default instead of faulting.
+ * buffer return the default instead of faulting.  A binding whose bit is set in
+ * D.instance_rate (Vulkan draw parameters only) steps by the instance index.
  */
-__device__ __forceinline__ float4 vgx_fetch(const VgxDraw &D, u32 loc, u32 index)
+__device__ __forceinline__ float4 vgx_fetch(const VgxDraw &D, u32 loc, u32 vertex, u32 instance)
 {
   float4 out = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
   if(loc >= VGX_MAX_ATTRS)
@@ -32,6 +33,7 @@ __device__ __forceinline__ float4 vgx_fetch(const VgxDraw &D, u32 loc, u32 index
   const VgxAttr a = D.attrs[loc];
   if(a.format == VGX_FMT_NONE || a.binding >= VGX_MAX_VB)
     return out;
+  const u32 index = ((D.instance_rate >> a.binding) & 1u) ? instance : vertex;
   u64 off = (u64)a.offset + (u64)a.stride * (u64)index;
   u32 size = a.format == VGX_FMT_RGBA32 ? 16u : a.format == VGX_FMT_RGB32 ? 12u
              : a.format == VGX_FMT_RG32 ? 8u : 4u;

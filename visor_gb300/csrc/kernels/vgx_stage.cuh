@@ -6,7 +6,7 @@
  *   VGX_K          interpolated float slots the fragment shader reads
  *   VGX_LOD_SLOT   slot of the sampled uv (-1: none) used for the trilinear LOD
  *   VGX_LOD_TEX    texture slot whose size scales that LOD
- *   vgx_vs(D, vertex_index, pos, out[VGX_K])
+ *   vgx_vs(D, vertex_index, instance_index, pos, out[VGX_K])
  *   vgx_fs(D, bary[4], i0, i1, i2, lod) -> float4
  *
  * vgx_setup  one thread per triangle: index fetch, 3 vertex-shader calls
@@ -189,10 +189,20 @@ __device__ __forceinline__ void vgx_warp_add_u64(u64 *dst, u64 v)
 
 /* Vertex indices of triangle `local` of a draw (ShadeVerts, rasterizer.cpp:100-232:
    lists take three consecutive elements, strips swap the first two of odd
-   triangles); returns true when an index lies outside the bound index buffer
-   (its vertex is then vertex 0). */
-__device__ __forceinline__ bool vgx_tri_indices(const VgxDraw &D, u32 local, u32 *idx)
+   triangles) and its instance index.  Instances follow one another, each the
+   whole primitive list, and indexed draws add vertex_offset to the fetched
+   indices (both only with Vulkan draw parameters; otherwise instances is 1 and
+   the offsets 0).  Returns true when an index lies outside the bound index
+   buffer (its vertex is then vertex 0). */
+__device__ __forceinline__ bool vgx_tri_indices(const VgxDraw &D, u32 local, u32 *idx, u32 &instance)
 {
+  instance = D.first_instance;
+  if(D.instances > 1u)
+  {
+    const u32 i = local / D.instance_tris;
+    local -= i * D.instance_tris;
+    instance += i;
+  }
   u32 vi[3];
   if(D.topology == VGX_TOPO_STRIP)
   {
@@ -221,8 +231,9 @@ __device__ __forceinline__ bool vgx_tri_indices(const VgxDraw &D, u32 local, u32
       }
       else
       {
-        idx[k] = D.index_type == VGX_INDEX_U16 ? (u32)__ldg((const u16 *)D.ib + e)
-                                               : __ldg((const u32 *)D.ib + e);
+        idx[k] = (D.index_type == VGX_INDEX_U16 ? (u32)__ldg((const u16 *)D.ib + e)
+                                                : __ldg((const u32 *)D.ib + e)) +
+                 (u32)D.vertex_offset;
       }
     }
   }
@@ -259,13 +270,13 @@ extern "C" __global__ void __launch_bounds__(256, 4) vgx_setup(VgxJob job)
     tbase = T.tile_base;
     tcols = T.tiles_x;
     const u32 local = tri - D.tri_base;
-    u32 vidx[3];
-    const bool bad = vgx_tri_indices(D, local, vidx);
+    u32 vidx[3], inst;
+    const bool bad = vgx_tri_indices(D, local, vidx, inst);
     float4 pos[3];
     float iv[3][VGX_K > 0 ? VGX_K : 1];
 #pragma unroll
     for(int k = 0; k < 3; k++)
-      vgx_vs(D, vidx[k], pos[k], iv[k]);
+      vgx_vs(D, vidx[k], inst, pos[k], iv[k]);
     if(bad)
       atomicOr((u32 *)job.status, VGX_STATUS_BAD_INDEX);
 
@@ -1211,13 +1222,13 @@ __device__ __forceinline__ void vgx_shade_deferred(const VgxJob &job, int lane, 
     const VgxDraw &D = draws[h[R_DRAW]];
     float iv[3][VGX_K > 0 ? VGX_K : 1];
 #if VGX_DEFERRED == 2
-    u32 vidx[3];
-    (void)vgx_tri_indices(D, rec - D.tri_base, vidx);
+    u32 vidx[3], inst;
+    (void)vgx_tri_indices(D, rec - D.tri_base, vidx, inst);
 #pragma unroll
     for(int v = 0; v < 3; v++)
     {
       float4 pos;
-      vgx_vs(D, vidx[v], pos, iv[v]);
+      vgx_vs(D, vidx[v], inst, pos, iv[v]);
     }
 #else
     {

@@ -95,6 +95,15 @@ typedef struct VgxDraw {
   u32 num_tris;
   u32 topology;
   u32 target;
+  /* Draw parameters.  The reference ignores vertexOffset, instanceCount and
+     firstInstance and fetches every attribute per vertex (cmd_exec.cpp:129-142);
+     that is instances 1 and the rest 0.  With Vulkan draw parameters the draw's
+     triangles run instance by instance, instance_tris at a time. */
+  i32 vertex_offset;  /* added to every fetched index (indexed draws) */
+  u32 first_instance; /* instance index of the first instance */
+  u32 instances;      /* instances drawn (num_tris = instances * instance_tris) */
+  u32 instance_tris;  /* triangles of one instance */
+  u32 instance_rate;  /* bit b: binding b steps once per instance */
   u32 cull_mode, front_face, depth_op, depth_write;
   u32 blend_enable, src_factor, dst_factor, blend_op;
   VgxAttr attrs[VGX_MAX_ATTRS]; /* indexed by location */

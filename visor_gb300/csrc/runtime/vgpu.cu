@@ -1248,6 +1248,9 @@ static int list_build(vgpu_list *l)
     /* draw */
     u32 ntris = c.draw.num_tris;
     l->tris_in += ntris;
+    /* job triangle ids are 32-bit: a job takes at most 2^31 triangles */
+    if(open && (u64)open->num_tris + ntris > (1ull << 31))
+      close_job();
     const bool same_code = open && (open->prog == c.prog || (open->prog->hash == c.prog->hash &&
                                                               open->prog->source == c.prog->source));
     if(!open || !batched || !same_code)

@@ -335,7 +335,8 @@ static int make_pipeline(vsd_scene *s, const vsc_pipeline &p, VkPipeline *out)
   }
   vsc_attr attrs[4];
   uint32_t na = vsc_vertex_attrs(p.shader, attrs);
-  VkVertexInputBindingDescription bind = {0, vsc_stride_of(p.shader), VK_VERTEX_INPUT_RATE_VERTEX};
+  VkVertexInputBindingDescription bind[2] = {{0, vsc_stride_of(p.shader), VK_VERTEX_INPUT_RATE_VERTEX},
+                                             {1, 0, VK_VERTEX_INPUT_RATE_INSTANCE}};
   VkVertexInputAttributeDescription vad[4];
   for(uint32_t i = 0; i < na; i++)
   {
@@ -343,11 +344,19 @@ static int make_pipeline(vsd_scene *s, const vsc_pipeline &p, VkPipeline *out)
     vad[i].binding = 0;
     vad[i].format = (VkFormat)attrs[i].format;
     vad[i].offset = attrs[i].offset;
+    if(p.instance_attr == attrs[i].location + 1)
+    {
+      /* this attribute alone, tightly packed, steps per instance from binding 1 */
+      vad[i].binding = 1;
+      vad[i].offset = 0;
+      bind[1].stride = attrs[i].format == 37 ? 4 : attrs[i].format == 100 ? 4 : attrs[i].format == 103 ? 8
+                       : attrs[i].format == 106 ? 12 : 16;
+    }
   }
   VkPipelineVertexInputStateCreateInfo vi = {};
   vi.sType = VK_STRUCTURE_TYPE_PIPELINE_VERTEX_INPUT_STATE_CREATE_INFO;
-  vi.vertexBindingDescriptionCount = 1;
-  vi.pVertexBindingDescriptions = &bind;
+  vi.vertexBindingDescriptionCount = p.instance_attr ? 2 : 1;
+  vi.pVertexBindingDescriptions = bind;
   vi.vertexAttributeDescriptionCount = na;
   vi.pVertexAttributeDescriptions = vad;
   VkPipelineInputAssemblyStateCreateInfo ia = {};
@@ -468,16 +477,18 @@ static int record(vsd_scene *s)
           cur_set = set;
         }
       }
-      VkDeviceSize off = d.vb_offset;
-      f.vkCmdBindVertexBuffers(s->cmd, 0, 1, &s->vb, &off);
+      VkDeviceSize off[2] = {d.vb_offset, d.inst_vb_offset};
+      VkBuffer vbs[2] = {s->vb, s->vb};
+      f.vkCmdBindVertexBuffers(s->cmd, 0, p.instance_attr ? 2 : 1, vbs, off);
       if(d.push_size)
         f.vkCmdPushConstants(s->cmd, s->layout,
                              VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0,
                              d.push_size, d.push);
+      const uint32_t instances = d.instances == VSC_NONE ? 0 : d.instances ? d.instances : 1;
       if(d.indexed)
-        f.vkCmdDrawIndexed(s->cmd, d.count, 1, d.first, 0, 0);
+        f.vkCmdDrawIndexed(s->cmd, d.count, instances, d.first, d.vertex_offset, d.first_instance);
       else
-        f.vkCmdDraw(s->cmd, d.count, 1, d.first, 0);
+        f.vkCmdDraw(s->cmd, d.count, instances, d.first, d.first_instance);
     }
     f.vkCmdEndRenderPass(s->cmd);
   }

@@ -387,7 +387,8 @@ uint32_t vsc_stride_of(uint32_t shader)
   {
     case VSC_SHADER_LAMBERT_TEX:
     case VSC_SHADER_CUBE: return VSC_STRIDE_LAMBERT_TEX;
-    case VSC_SHADER_COLOR: return VSC_STRIDE_COLOR;
+    case VSC_SHADER_COLOR:
+    case VSC_SHADER_COLOR_INSTANCED: return VSC_STRIDE_COLOR;
     case VSC_SHADER_LAMBERT_TEX_ALPHA: return VSC_STRIDE_LAMBERT_TEX_ALPHA;
     default: return 0;
   }
@@ -408,6 +409,7 @@ uint32_t vsc_vertex_attrs(uint32_t shader, vsc_attr *a)
       a[3].location = 3; a[3].format = 100; a[3].offset = 32; /* alpha */
       return 4;
     case VSC_SHADER_COLOR:
+    case VSC_SHADER_COLOR_INSTANCED:
       a[0].location = 0; a[0].format = 109; a[0].offset = 0;  /* clip-space position */
       a[1].location = 1; a[1].format = 37; a[1].offset = 16;  /* RGBA8 colour */
       return 2;

@@ -20,13 +20,14 @@ enum {
   OpTypeImage = 25, OpTypeSampledImage = 27, OpTypeStruct = 30, OpTypePointer = 32,
   OpTypeFunction = 33, OpConstant = 43, OpFunction = 54, OpFunctionEnd = 56, OpVariable = 59,
   OpLoad = 61, OpStore = 62, OpAccessChain = 65, OpDecorate = 71, OpMemberDecorate = 72,
-  OpVectorShuffle = 79, OpCompositeConstruct = 80, OpCompositeExtract = 81,
+  OpVectorShuffle = 79, OpCompositeConstruct = 80, OpCompositeExtract = 81, OpCompositeInsert = 82,
+  OpConvertSToF = 111, OpFAdd = 129, OpFMul = 133,
   OpImageSampleImplicitLod = 87, OpVectorTimesScalar = 142, OpMatrixTimesVector = 145,
   OpDot = 148, OpLabel = 248, OpReturn = 253,
 };
 enum { DecBlock = 2, DecColMajor = 5, DecMatrixStride = 7, DecBuiltIn = 11, DecLocation = 30,
        DecBinding = 33, DecDescriptorSet = 34, DecOffset = 35 };
-enum { BuiltInPosition = 0, BuiltInPointSize = 1 };
+enum { BuiltInPosition = 0, BuiltInPointSize = 1, BuiltInInstanceIndex = 43 };
 enum { SCUniformConstant = 0, SCInput = 1, SCOutput = 3, SCFunction = 7, SCPushConstant = 9 };
 enum { GLSLFMax = 40, GLSLNormalize = 69 };
 
@@ -382,7 +383,8 @@ static size_t emit_lambert_fs(int alpha, uint32_t *words, size_t cap)
                 iface, ni, 1, words, cap);
 }
 
-static size_t emit_color_vs(uint32_t *words, size_t cap)
+/* gl_Position = inPos (instanced: inPos.x += float(gl_InstanceIndex) * 0.25); colour passed on */
+static size_t emit_color_vs(int instanced, uint32_t *words, size_t cap)
 {
   mod m;
   common c;
@@ -395,19 +397,39 @@ static size_t emit_color_vs(uint32_t *words, size_t cap)
   decorate_loc(&m, inPos, 0);
   decorate_loc(&m, inCol, 1);
   decorate_loc(&m, outCol, 0);
+  uint32_t inInst = 0, quarter = 0;
+  if(instanced)
+  {
+    inInst = var(&m, ptr(&m, SCInput, c.tint), SCInput);
+    I(&m.annot, OpDecorate, inInst, DecBuiltIn, BuiltInInstanceIndex);
+    quarter = m.next++;
+    I(&m.types, OpConstant, c.tfloat, quarter, fbits(0.25f));
+  }
   buf *f = &m.code;
   I(f, OpFunction, c.tvoid, c.main, 0, c.tfn);
   I(f, OpLabel, m.next++);
   uint32_t p = m.next++, gp = m.next++, col = m.next++;
   I(f, OpLoad, c.vec4, p, inPos);
+  if(instanced)
+  {
+    uint32_t ii = m.next++, fi = m.next++, dx = m.next++, x = m.next++, x2 = m.next++, p2 = m.next++;
+    I(f, OpLoad, c.tint, ii, inInst);
+    I(f, OpConvertSToF, c.tfloat, fi, ii);
+    I(f, OpFMul, c.tfloat, dx, fi, quarter);
+    I(f, OpCompositeExtract, c.tfloat, x, p, 0);
+    I(f, OpFAdd, c.tfloat, x2, x, dx);
+    I(f, OpCompositeInsert, c.vec4, p2, x2, p, 0);
+    p = p2;
+  }
   I(f, OpAccessChain, pvo4, gp, pv, c.int0);
   I(f, OpStore, gp, p);
   I(f, OpLoad, c.vec4, col, inCol);
   I(f, OpStore, outCol, col);
   inst(f, OpReturn, 0, NULL);
   inst(f, OpFunctionEnd, 0, NULL);
-  uint32_t iface[4] = {pv, inPos, inCol, outCol};
-  return finish(&m, &c, 0, "visor_shader:color.vert", iface, 4, 0, words, cap);
+  uint32_t iface[5] = {pv, inPos, inCol, outCol, inInst};
+  return finish(&m, &c, 0, instanced ? "visor_shader:color_instanced.vert" : "visor_shader:color.vert", iface,
+                instanced ? 5 : 4, 0, words, cap);
 }
 
 static size_t emit_color_fs(uint32_t *words, size_t cap)
@@ -474,7 +496,10 @@ size_t vspv_emit(uint32_t shader, uint32_t stage, uint32_t *words, size_t capaci
       return stage == VSPV_STAGE_VERTEX ? emit_lambert_vs(1, words, capacity)
                                         : emit_lambert_fs(1, words, capacity);
     case VSC_SHADER_COLOR:
-      return stage == VSPV_STAGE_VERTEX ? emit_color_vs(words, capacity)
+      return stage == VSPV_STAGE_VERTEX ? emit_color_vs(0, words, capacity)
+                                        : emit_color_fs(words, capacity);
+    case VSC_SHADER_COLOR_INSTANCED:
+      return stage == VSPV_STAGE_VERTEX ? emit_color_vs(1, words, capacity)
                                         : emit_color_fs(words, capacity);
     case VSC_SHADER_CUBE:
       return stage == VSPV_STAGE_VERTEX ? emit_lambert_vs(0, words, capacity)

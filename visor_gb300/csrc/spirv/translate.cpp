@@ -1619,7 +1619,8 @@ bool translate(const Module *vs, const char *vs_entry, const Module *fs, const c
   src << gv.out.str() << gf.out.str();
 
   /* vertex wrapper */
-  src << "__device__ __forceinline__ void vgx_vs(const VgxDraw &D, u32 vertex_index, float4 &pos, float *out)\n{\n";
+  src << "__device__ __forceinline__ void vgx_vs(const VgxDraw &D, u32 vertex_index, u32 instance_index, "
+         "float4 &pos, float *out)\n{\n";
   src << "  vs_Ctx ctx;\n  ctx.D = &D;\n  ctx.lod = 0.0f;\n";
   std::map<uint32_t, uint32_t> vs_out_loc; /* location -> var */
   std::string pos_expr;
@@ -1639,7 +1640,9 @@ bool translate(const Module *vs, const char *vs_entry, const Module *fs, const c
         if(bi == BI_VertexIndex || bi == BI_VertexId)
           src << "  ctx.g" << vid << " = (" << gv.ctype(ty) << ")vertex_index;\n";
         else if(bi == BI_InstanceIndex || bi == BI_InstanceId)
-          src << "  ctx.g" << vid << " = 0;\n";
+          /* the reference stores 0 (spirv_compile.cpp:1946-1949); the draw's
+             first_instance is 0 there too, unless Vulkan draw parameters are on */
+          src << "  ctx.g" << vid << " = (" << gv.ctype(ty) << ")instance_index;\n";
         else
         {
           err = "unsupported vertex built-in input";
@@ -1649,7 +1652,7 @@ bool translate(const Module *vs, const char *vs_entry, const Module *fs, const c
       }
       if(!get_dec(*vs, vid, D_Location, &loc))
         continue;
-      src << "  { float4 a_ = vgx_fetch(D, " << loc << "u, vertex_index); float f_[4] = {a_.x, a_.y, a_.z, a_.w};";
+      src << "  { float4 a_ = vgx_fetch(D, " << loc << "u, vertex_index, instance_index); float f_[4] = {a_.x, a_.y, a_.z, a_.w};";
       bool isint = t.k == K_INT || (t.k == K_VEC && vs->types.at(t.elem).k == K_INT);
       uint32_t n = t.k == K_VEC ? t.count : 1;
       for(uint32_t i = 0; i < n; i++)

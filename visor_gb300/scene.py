@@ -12,6 +12,7 @@ SHADER_LAMBERT_TEX = 1
 SHADER_COLOR = 2
 SHADER_LAMBERT_TEX_ALPHA = 3
 SHADER_CUBE = 4
+SHADER_COLOR_INSTANCED = 5
 
 TEXFMT_RGBA8, TEXFMT_BC2, TEXFMT_BC3 = 0, 1, 2
 
@@ -38,7 +39,7 @@ NONE = 0xFFFFFFFF
 class Pipeline(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in (
         "shader", "topology", "cull_mode", "front_face", "depth_test", "depth_op", "depth_write",
-        "blend_enable", "src_factor", "dst_factor", "filter")]
+        "blend_enable", "src_factor", "dst_factor", "filter", "instance_attr")]
 
 
 class Texture(C.Structure):
@@ -54,7 +55,9 @@ class Target(C.Structure):
 class Draw(C.Structure):
     _fields_ = [("pipeline", C.c_uint32), ("texture", C.c_uint32), ("indexed", C.c_uint32),
                 ("count", C.c_uint32), ("first", C.c_uint32), ("push_size", C.c_uint32),
-                ("vb_offset", C.c_uint64), ("push", C.c_uint8 * 128)]
+                ("vb_offset", C.c_uint64), ("push", C.c_uint8 * 128), ("vertex_offset", C.c_int32),
+                ("instances", C.c_uint32), ("first_instance", C.c_uint32), ("reserved", C.c_uint32),
+                ("inst_vb_offset", C.c_uint64)]
 
 
 class Pass(C.Structure):
@@ -176,11 +179,18 @@ def make_pipeline(shader, **kw):
     p.src_factor = kw.get("src_factor", BLEND_ONE)
     p.dst_factor = kw.get("dst_factor", BLEND_ZERO)
     p.filter = kw.get("filter", FILTER_REFERENCE)
+    p.instance_attr = kw.get("instance_attr", 0)
     return p
 
 
-def make_draw(pipeline, count, first=0, indexed=False, texture=NONE, vb_offset=0, push=b""):
+def make_draw(pipeline, count, first=0, indexed=False, texture=NONE, vb_offset=0, push=b"",
+              vertex_offset=0, instances=0, first_instance=0, inst_vb_offset=0):
+    """A scene draw; the last four are Vulkan draw parameters (instances 0 records 1)."""
     d = Draw()
+    d.vertex_offset = vertex_offset
+    d.instances = instances
+    d.first_instance = first_instance
+    d.inst_vb_offset = inst_vb_offset
     d.pipeline = pipeline
     d.texture = texture
     d.indexed = 1 if indexed else 0
