@@ -1,0 +1,22 @@
+"""Autotuner choice rule (host logic, no GPU)."""
+from visor_gb300 import tune
+
+
+def test_fastest_wins_outside_the_tie_band():
+    times = {(3, 1): 2.39, (4, 4): 1.60, (5, 16): 1.53}
+    assert tune.pick(times, tune.CANDIDATES) == (5, 16)
+
+
+def test_near_tie_goes_to_the_earlier_candidate():
+    # two runs of the 1M-triangle scene: 16x16/4 and 32x32/16 came out 0.1-0.5 % apart,
+    # each ahead once; both now tune to the same configuration
+    run_a = {(3, 1): 2.3939, (4, 1): 7.848, (4, 4): 1.5187, (5, 4): 8.6147, (5, 8): 3.1293, (5, 16): 1.5315}
+    run_b = {(3, 1): 2.3944, (4, 1): 7.8781, (4, 4): 1.5421, (5, 4): 8.6126, (5, 8): 3.185, (5, 16): 1.5343}
+    assert tune.pick(run_a, tune.CANDIDATES) == (4, 4)
+    assert tune.pick(run_b, tune.CANDIDATES) == (4, 4)
+
+
+def test_custom_candidate_order():
+    times = {(5, 16): 1.000, (4, 4): 1.005}
+    assert tune.pick(times, [(5, 16), (4, 4)]) == (5, 16)
+    assert tune.pick(times, [(4, 4), (5, 16)]) == (4, 4)

@@ -12,6 +12,17 @@ import visor_gb300 as vg
 # (log2 bin edge, warps per bin): 8x8 ... 64x64 bins, 1 ... 16 warps
 CANDIDATES = [(3, 1), (4, 1), (4, 4), (5, 4), (5, 8), (5, 16), (6, 8), (6, 16)]
 
+# Candidates within this fraction of the fastest are timing noise apart; the first
+# of them in candidate order (smaller bins, fewer warps) is chosen, so that a scene
+# tunes to the same configuration from run to run.
+TIE = 0.01
+
+
+def pick(results, order):
+    """The first candidate of `order` within TIE of the fastest time in `results`."""
+    best = min(results.values())
+    return next(c for c in order if c in results and results[c] <= best * (1.0 + TIE))
+
 
 def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
     """Return (best (bin_shift, warps), {candidate: ms}) for a scene on a device."""
@@ -31,6 +42,6 @@ def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
             results[(shift, warps)] = best
     finally:
         up.release()
-    choice = min(results, key=results.get)
+    choice = pick(results, candidates or CANDIDATES)
     vg.set_tuning(bin_shift=choice[0], raster_warps=choice[1])
     return choice, results
