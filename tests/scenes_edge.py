@@ -339,6 +339,10 @@ SPEC_SCENES = {
                                     "textures": 4, "tex_size": 64}),
     "cfg5_request_trilinear": (5, 13, {"count": 2, "max_tris": 20000, "textures": 4,
                                        "tex_size": 128}),
+    # more triangles than pixels with trilinear sampling: the raster recomputes the
+    # interpolants and the triangle's LOD for the shaded fragments
+    "cfg3_dense_trilinear": (3, 19, {"width": 96, "height": 64, "count": 12, "min_tris": 1000,
+                                     "max_tris": 4000, "textures": 2, "tex_size": 64}),
 }
 
 

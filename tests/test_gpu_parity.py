@@ -71,7 +71,7 @@ VARIANT_SCENES = ["blend_overlap", "depth_lequal", "depth_less", "depth_equal", 
                   "depth_gequal", "depth_not_equal", "depth_always", "degenerate", "shared_edges", "offscreen",
                   "guard_band", "guard_band_blend", "corner_sliver", "strip",
                   "texture_wrap", "load_pass",
-                  "cfg1_sphere", "cfg2_small_blend", "cfg3_small_trilinear", "cfg4_small"]
+                  "cfg1_sphere", "cfg2_small_blend", "cfg3_small_trilinear", "cfg3_dense_trilinear", "cfg4_small"]
 
 
 @pytest.mark.parametrize("variant", [(4, 1, 0), (4, 4, 0), (5, 8, 0), (5, 16, 0), (6, 16, 0), (3, 1, 1), (4, 4, 1),
