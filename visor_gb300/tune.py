@@ -3,7 +3,9 @@
 Every candidate renders the same pixels (the configuration only changes how
 work is binned and distributed), so the tuner may time candidates on the real
 command buffer.  Each candidate lowers the command buffer again, replays it a
-few times and keeps the fastest device time (CUDA events around the submit).
+few times and keeps the fastest device time (CUDA events around the submit),
+with L2 flushed before every replay as in the benchmark's timed loop (a warm L2
+favours large bin tiles, whose pair lists it holds).
 The scene is uploaded once: a command buffer's list is formed again on the
 first submit after the bin tile or warp count changes.
 """
@@ -35,6 +37,7 @@ def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
             up.submit()
             best = None
             for _ in range(reps):
+                dev.flush_l2()
                 dev.reset_stats()
                 up.submit()
                 ms = dev.stats()["gpu_ms"]
