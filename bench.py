@@ -380,7 +380,7 @@ def measure_config(dev, h, steps, warmup, modes=("batched", "per_draw")):
     import visor_gb300 as vg
     from visor_gb300 import tune
     out = {}
-    choice, tuned = tune.tune(dev, h, vg.DEVICE_TARGETS, reps=2)
+    choice, tuned = tune.tune(dev, h, vg.DEVICE_TARGETS, reps=3)
     out["tuning"] = {"bin_tile": 1 << choice[0], "warps_per_bin": choice[1],
                      "ms": {f"{1 << k[0]}x{1 << k[0]}/{k[1]}w": round(v, 4) for k, v in tuned.items()}}
     for name in modes:

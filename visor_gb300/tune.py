@@ -3,9 +3,10 @@
 Every candidate renders the same pixels (the configuration only changes how
 work is binned and distributed), so the tuner may time candidates on the real
 command buffer.  Each candidate lowers the command buffer again, replays it a
-few times and keeps the fastest device time (CUDA events around the submit),
-with L2 flushed before every replay as in the benchmark's timed loop (a warm L2
-favours large bin tiles, whose pair lists it holds).
+few times and scores the mean device time (CUDA events around the submit), with
+L2 flushed before every replay: the statistic and conditions of the benchmark's
+timed loop (a warm L2, or the fastest of a few replays, favours large bin tiles,
+whose times spread more).
 The scene is uploaded once: a command buffer's list is formed again on the
 first submit after the bin tile or warp count changes.
 """
@@ -26,7 +27,7 @@ def pick(results, order):
     return next(c for c in order if c in results and results[c] <= best * (1.0 + TIE))
 
 
-def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
+def tune(dev, handle, flags=0, candidates=None, reps=5, mode=vg.MODE_BATCHED):
     """Return (best (bin_shift, warps), {candidate: ms}) for a scene on a device."""
     results = {}
     vg.set_mode(mode)
@@ -35,14 +36,13 @@ def tune(dev, handle, flags=0, candidates=None, reps=3, mode=vg.MODE_BATCHED):
         for shift, warps in candidates or CANDIDATES:
             vg.set_tuning(bin_shift=shift, raster_warps=warps)
             up.submit()
-            best = None
+            times = []
             for _ in range(reps):
                 dev.flush_l2()
                 dev.reset_stats()
                 up.submit()
-                ms = dev.stats()["gpu_ms"]
-                best = ms if best is None else min(best, ms)
-            results[(shift, warps)] = best
+                times.append(dev.stats()["gpu_ms"])
+            results[(shift, warps)] = sum(times) / len(times)
     finally:
         up.release()
     choice = pick(results, candidates or CANDIDATES)
