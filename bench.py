@@ -507,7 +507,9 @@ def serving_sweep(dev, rates, seconds, pool_size, budget, slots):
                 "mean_batch": float(batch.mean()), "batches": st1["batches"] - st0["batches"],
                 "shaded_gfrags_per_s": (st1["shaded"] - st0["shaded"]) / span / 1e9,
                 "mtris_per_s": (st1["tris"] - st0["tris"]) / span / 1e6,
-                "peak_reserved_gb": st1["peak_reserved_bytes"] / 1e9})
+                "peak_reserved_gb": st1["peak_reserved_bytes"] / 1e9,
+                # longest host time one batch took to launch, since the server started
+                "max_launch_ms_so_far": st1["max_launch_ns"] / 1e6})
     finally:
         srv.close()
         for b in ring:

@@ -191,6 +191,8 @@ typedef struct vgpu_server_stats {
   uint32_t max_batch_seen, in_flight;
   uint64_t tris, shaded;                        /* over completed batches */
   uint64_t peak_device_bytes;                   /* peak of admitted requests' bytes + binning storage */
+  uint64_t max_launch_ns;                       /* longest host time to launch one batch: admission,
+                                                   list build, storage growth, enqueue of its kernels */
 } vgpu_server_stats;
 
 int vgpu_server_create(const vgpu_server_config *cfg, vgpu_server **out);

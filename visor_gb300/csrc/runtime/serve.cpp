@@ -256,6 +256,7 @@ void finish_batch(vgpu_server *S, Slot &sl)
 /* Admit queued requests into a free slot and queue stage 1. */
 void launch_batch(vgpu_server *S, Slot &sl)
 {
+  const uint64_t t_start = vgpu_now_ns();
   {
     std::lock_guard<std::mutex> g(S->mu);
     uint64_t tris = 0;
@@ -353,6 +354,9 @@ void launch_batch(vgpu_server *S, Slot &sl)
     return;
   }
   sl.stage = 1;
+  const uint64_t dt = vgpu_now_ns() - t_start;
+  std::lock_guard<std::mutex> g(S->mu);
+  S->stats.max_launch_ns = std::max(S->stats.max_launch_ns, dt);
 }
 
 void scheduler(vgpu_server *S)
