@@ -508,7 +508,9 @@ def serving_sweep(dev, rates, seconds, pool_size, budget, slots):
                 "shaded_gfrags_per_s": (st1["shaded"] - st0["shaded"]) / span / 1e9,
                 "mtris_per_s": (st1["tris"] - st0["tris"]) / span / 1e6,
                 "peak_reserved_gb": st1["peak_reserved_bytes"] / 1e9,
-                # longest host time one batch took to launch, since the server started
+                # host time the scheduler spent launching a batch: mean at this rate, and the
+                # longest since the server started (its first batches load kernels)
+                "mean_launch_ms": (st1["launch_ns"] - st0["launch_ns"]) / max(1, st1["batches"] - st0["batches"]) / 1e6,
                 "max_launch_ms_so_far": st1["max_launch_ns"] / 1e6})
     finally:
         srv.close()

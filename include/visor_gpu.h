@@ -193,6 +193,7 @@ typedef struct vgpu_server_stats {
   uint64_t peak_device_bytes;                   /* peak of admitted requests' bytes + binning storage */
   uint64_t max_launch_ns;                       /* longest host time to launch one batch: admission,
                                                    list build, storage growth, enqueue of its kernels */
+  uint64_t launch_ns;                           /* that host time summed over launched batches */
 } vgpu_server_stats;
 
 int vgpu_server_create(const vgpu_server_config *cfg, vgpu_server **out);

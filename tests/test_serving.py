@@ -178,7 +178,7 @@ def test_budget_bounds_admission(device, pool):
     # admitted requests plus the slots' binning storage (grown for a batch's bin tiles
     # before it runs) never exceed the budget
     assert stats["peak_device_bytes"] <= budget
-    assert stats["completed"] == 0 or stats["max_launch_ns"] > 0
+    assert stats["completed"] == 0 or 0 < stats["max_launch_ns"] <= stats["launch_ns"]
     assert stats["peak_reserved_bytes"] <= budget - binning
     for k, i in enumerate(order):
         _assert_frame(pool[i], frames[k], f"request {i}")

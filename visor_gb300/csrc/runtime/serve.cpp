@@ -357,6 +357,7 @@ void launch_batch(vgpu_server *S, Slot &sl)
   const uint64_t dt = vgpu_now_ns() - t_start;
   std::lock_guard<std::mutex> g(S->mu);
   S->stats.max_launch_ns = std::max(S->stats.max_launch_ns, dt);
+  S->stats.launch_ns += dt;
 }
 
 void scheduler(vgpu_server *S)

@@ -48,7 +48,7 @@ class ServerStats(C.Structure):
                 ("peak_reserved_bytes", C.c_uint64), ("binning_bytes", C.c_uint64),
                 ("max_batch_seen", C.c_uint32), ("in_flight", C.c_uint32),
                 ("tris", C.c_uint64), ("shaded", C.c_uint64), ("peak_device_bytes", C.c_uint64),
-                ("max_launch_ns", C.c_uint64)]
+                ("max_launch_ns", C.c_uint64), ("launch_ns", C.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
