@@ -156,6 +156,33 @@ def _no_draws(k):
     return {n: v for n, v in k.items() if n != "draws"}
 
 
+def test_scene_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the scene's draw and pipeline have the layout of include/visor_scene.h."""
+    import ctypes
+    import os
+    import subprocess
+    from conftest import REPO
+    checks = {"vsc_draw": vs.Draw, "vsc_pipeline": vs.Pipeline}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "visor_scene.h"', "int main(void) {"]
+    for cname, py in checks.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for cname, py in checks.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
 def test_switch_round_trip():
     was = vg.draw_parameters()
     try:
