@@ -498,12 +498,16 @@ def serving_sweep(dev, rates, seconds, pool_size, budget, slots):
             done += srv.poll(4096)
             st1 = srv.stats()
             lat = np.array([(c["done_ns"] - c["arrival_ns"]) / 1e6 for c in done if c["status"] == 0])
+            # where the latency accrues: arrival to admission into a batch, admission to result
+            wait = np.array([(c["admit_ns"] - c["arrival_ns"]) / 1e6 for c in done if c["status"] == 0])
+            service = np.array([(c["done_ns"] - c["admit_ns"]) / 1e6 for c in done if c["status"] == 0])
             batch = np.array([c["batch_size"] for c in done])
             span = (max(c["done_ns"] for c in done) - t0) / 1e9
             out["rates"].append({
                 "rate_per_s": rate, "requests": n, "completed": int(len(lat)),
                 "frames_per_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "p99_wait_ms": float(np.percentile(wait, 99)), "p99_service_ms": float(np.percentile(service, 99)),
                 "mean_batch": float(batch.mean()), "batches": st1["batches"] - st0["batches"],
                 "shaded_gfrags_per_s": (st1["shaded"] - st0["shaded"]) / span / 1e9,
                 "mtris_per_s": (st1["tris"] - st0["tris"]) / span / 1e6,
