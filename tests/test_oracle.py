@@ -77,6 +77,11 @@ def test_oracle_equals_reference_fresh_seeds(oracle, seed):
         (vs.CFG_TRIS, dict(width=200, height=150, count=1500, max_area=3000.0)),
         (vs.CFG_SPHERE, dict(width=160, height=120, count=2)),
         (vs.CFG_TARGETS, dict(count=3, min_tris=100, max_tris=2000, width=64, height=48)),
+        (vs.CFG_DRAWS, dict(width=160, height=100, count=10, max_tris=800, textures=2, tex_size=32,
+                            flags=vs.FLAG_FILTER_REFERENCE)),
+        (vs.CFG_TRIS, dict(width=128, height=96, count=800, max_area=1500.0,
+                           flags=vs.FLAG_NO_BLEND | vs.FLAG_CLOCKWISE)),
+        (vs.CFG_SERVING, dict(count=1, max_tris=3000, textures=2, tex_size=64, flags=vs.FLAG_FILTER_REFERENCE)),
     ]
     for cfg, params in cases:
         ho = oracle.generate(cfg, seed, **params)
