@@ -228,6 +228,23 @@ def test_cases_depend_on_draw_parameters(name):
     assert any(not np.array_equal(x, y) for x, y in zip(a[0] + a[1], b[0] + b[1]))
 
 
+@pytest.mark.parametrize("name", list(CASES))
+def test_expanded_scenes_pinned_to_reference(name):
+    """The equivalent scenes the GPU output is compared with render the same in the
+    reference build as in the oracle, so each Vulkan-semantics image is pinned to the
+    reference's own rasterizer too."""
+    try:
+        ref = loader.Reference()
+    except OSError:
+        pytest.skip("reference build not present")
+    o = loader.Oracle()
+    oc, od, ok = o.render(_build(o.lib, name, "expanded"))
+    rc, rd, rk, _ = ref.render(_build(ref.lib, name, "expanded"), threaded=False)
+    assert ok == rk
+    for a, b in zip(oc + od, rc + rd):
+        assert np.array_equal(a, b)
+
+
 @pytest.fixture(scope="module")
 def device():
     d = vg.Device()
